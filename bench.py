@@ -1,0 +1,468 @@
+#!/usr/bin/env python
+"""Benchmark: biharmonic smoothing on a 70^3 tet cube, setup + solve.
+
+Workload (one step): build the factored operator (alpha M + K M^-1 K) and an
+adaptive FSAI (width 8, single-entry growth, kap 1e-3) on the assembled
+Q = alpha M + K M^-1 K, then solve Q u = alpha M f for four right-hand sides
+(f = sin(3x) + cos(2y) z + x z, then the vertex x, y, z coordinates) with
+preconditioned CG to relative residual 1e-8, all in float64 on the GPU.
+Inputs are synthetic and seeded; assembly of K, M and Q happens once on the
+host and is not timed (as in the reference).
+
+Prints one JSON line.  `value` is solves/s with inputs resident on the device;
+`e2e` is the same metric through the public API starting from pinned host
+buffers (host->device copies of Q, K, mass and the right-hand sides and the
+device->host copy of the solutions inside the timed region).
+
+--impl reference times the reference algorithm's CPU restatement (the oracle,
+all host threads) on the same workload: a bounded sample (setup plus a fixed
+number of CG iterations per right-hand side) extrapolated to the iteration
+count that the CPU solve needs, measured once in the warm-up.
+
+Multi-GPU (--gpus N under torchrun): the path has no data exchange, so every
+rank solves its own replica of the workload ("replicas only"); `value` sums
+all ranks' solves over the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "setup+solve ms and solves/s at 1e-8 rel residual; apply GB/s; p50/p99 latency"
+ALPHA = 1e-4
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--side", type=int, default=70, help="vertices per cube edge")
+    p.add_argument("--width", type=int, default=8, help="FSAI max_row_size")
+    p.add_argument("--step-size", type=int, default=1, help="FSAI max_step_size")
+    p.add_argument("--method", choices=["cg", "cr"], default="cg")
+    p.add_argument("--rtol", type=float, default=1e-8)
+    p.add_argument("--cpu-iters", type=int, default=100,
+                   help="CG iterations per right-hand side in the CPU sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def build_problem(side):
+    from warp_preconditioners_gb300 import problems
+
+    t0 = time.perf_counter()
+    verts, tets, K, mass = problems.tet_cube(side)
+    Q = problems.biharmonic(K, mass, ALPHA)
+    rhs = problems.smoothing_rhs(verts, mass, ALPHA)
+    return dict(verts=verts, K=K, mass=mass, Q=Q, rhs=rhs, n=K.shape[0], ntets=len(tets),
+                assembly_s=time.perf_counter() - t0)
+
+
+def iteration_bytes(n, nnz_k, nnz_g, nnz_gt):
+    """Algorithmic bytes of one float64 PCG iteration (factored operator + FSAI)."""
+    spmv_k = 2 * (nnz_k * 12 + 4 * (n + 1)) + 5 * n * 8 + n * 8
+    fsai = (nnz_g + nnz_gt) * 12 + 2 * 4 * (n + 1) + 4 * n * 8
+    vectors = 9 * n * 8
+    return spmv_k + fsai + vectors
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def cpu_baseline_sample(prob, width, step_size, method, cpu_iters, iterations_per_rhs):
+    """Oracle (CPU restatement) on the host cores: FSAI setup + cpu_iters iterations."""
+    from oracle import oracle
+
+    o = oracle
+    Q, K, mass = prob["Q"], prob["K"], prob["mass"]
+    qc = o.CSR(Q.indptr, Q.indices, Q.data)
+    kc = o.CSR(K.indptr, K.indices, K.data)
+    t0 = time.perf_counter()
+    g, gt, _ = o.fsai(qc, width=width, step=step_size, tol=1e-3)
+    setup = time.perf_counter() - t0
+    A = o.Operator.sqlap(kc, mass, ALPHA)
+    M = o.Operator.fsai(g, gt)
+    t0 = time.perf_counter()
+    _, it, _, _ = o.krylov(method, A, prob["rhs"][0], M=M, tol=0.0, maxiter=cpu_iters)
+    per_iter = (time.perf_counter() - t0) / max(it, 1)
+    total = setup + per_iter * sum(iterations_per_rhs)
+    return dict(setup_s=setup, per_iteration_s=per_iter, total_s=total, threads=o.num_threads(),
+                iters_sampled=it)
+
+
+def run_reference(args, prob):
+    """The CPU restatement of the reference algorithm, all host threads."""
+    from oracle import oracle
+
+    threads = oracle.num_threads()
+    # Warm-up: one full CPU solve of the first right-hand side to learn the
+    # CPU iteration count used to extrapolate the bounded timed samples.
+    Q, K, mass = prob["Q"], prob["K"], prob["mass"]
+    qc = oracle.CSR(Q.indptr, Q.indices, Q.data)
+    kc = oracle.CSR(K.indptr, K.indices, K.data)
+    g, gt, _ = oracle.fsai(qc, width=args.width, step=args.step_size, tol=1e-3)
+    A = oracle.Operator.sqlap(kc, mass, ALPHA)
+    M = oracle.Operator.fsai(g, gt)
+    full_iters = []
+    for k in range(min(args.warmup, 1)):
+        _, it, _, _ = oracle.krylov(args.method, A, prob["rhs"][k], M=M, tol=args.rtol,
+                                    maxiter=200000)
+        full_iters.append(it)
+    if not full_iters:
+        _, it, _, _ = oracle.krylov(args.method, A, prob["rhs"][0], M=M, tol=args.rtol,
+                                    maxiter=200000)
+        full_iters.append(it)
+    its = [full_iters[0]] * 4
+    samples = []
+    for _ in range(args.steps):
+        s = cpu_baseline_sample(prob, args.width, args.step_size, args.method, args.cpu_iters, its)
+        samples.append(s["total_s"])
+    t = statistics.median(samples)
+    value = 4.0 / t
+    sample = (f"FSAI w{args.width} setup + {args.cpu_iters} PCG iterations of one RHS per step, "
+              f"extrapolated to {full_iters[0]} iterations x 4 RHS (iteration count from one "
+              f"full CPU solve in warm-up)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, prob),
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, prob):
+    Q = prob["Q"]
+    return {
+        "workload": f"biharmonic smoothing (alpha M + K M^-1 K) u = alpha M f on a {args.side}^3 "
+                    f"jittered tet cube; FSAI w{args.width} step {args.step_size} kap 1e-3 on the "
+                    f"assembled Q; factored operator; {args.method.upper()} to {args.rtol:g}; "
+                    f"4 RHS; float64",
+        "n": prob["n"], "tets": prob["ntets"], "nnz_K": int(prob["K"].nnz), "nnz_Q": int(Q.nnz),
+        "fsai_width": args.width, "max_step_size": args.step_size, "kap_tolerance": 1e-3,
+        "solver": args.method, "rhs": 4, "rel_tol": args.rtol,
+        "l2": "inputs larger than L2 (Q values+columns %.0f MB > 129 MB)" % (Q.nnz * 12 / 1e6),
+        "parallelism": f"replicas x{args.gpus}",
+    }
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        prob = build_problem(args.side)
+        run_reference(args, prob)
+        return
+
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, from_scipy, linear
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    prob = build_problem(args.side)
+    n = prob["n"]
+    Q = from_scipy(prob["Q"], dev)
+    K = from_scipy(prob["K"], dev)
+    mass = torch.as_tensor(prob["mass"], device=dev)
+    free = torch.arange(n, dtype=torch.int32, device=dev)
+    rhs = torch.as_tensor(prob["rhs"], device=dev).contiguous()
+    b = torch.empty(n, dtype=torch.float64, device=dev)
+    xs = torch.zeros((4, n), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def one_step(Qm, Km, massv, rhsv, out, rec=None):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        op = SquaredLaplacianOperator(Km, massv, free, mass_weight=ALPHA)
+        pre = FSAI(Qm, max_row_size=args.width, max_step_size=args.step_size,
+                   kap_tolerance=1e-3)
+        ev[0].record(stream)
+        solver = linear.Solver(args.method, op, pre)
+        its = []
+        for k in range(4):
+            b.copy_(rhsv[k])
+            out[k].zero_()
+            nit, rr, _ = solver.run(b, out[k], tol=args.rtol, maxiter=100000)
+            its.append(nit.clone())
+        ev[1].record(stream)
+        if rec is not None:
+            rec.append((ev, its, pre))
+        return pre
+
+    for _ in range(args.warmup):
+        one_step(Q, K, mass, rhs, xs)
+    torch.cuda.synchronize()
+
+    recs = []
+    with ClockSampler(local) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            one_step(Q, K, mass, rhs, xs, recs)
+        end.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    elapsed_ms = start.elapsed_time(end)
+    if dist:
+        t = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    solve_ms = [r[0][0].elapsed_time(r[0][1]) for r in recs]
+    setup_ms = [ms_per_step - s for s in solve_ms]
+    iters = [[int(i.item()) for i in r[1]] for r in recs]
+    value = 4.0 * args.steps * world / (elapsed_ms / 1e3)
+
+    # Accuracy of the last step against the assembled Q (float64, host).
+    qh = prob["Q"]
+    sols = xs.cpu().numpy()
+    relres = [float(np.linalg.norm(prob["rhs"][k] - qh @ sols[k]) / np.linalg.norm(prob["rhs"][k]))
+              for k in range(4)]
+    pre = recs[-1][2]
+    nnz_g, nnz_gt = pre.G.nnz, pre.GT.nnz
+    total_iters = sum(sum(i) for i in iters)
+    solve_total_s = sum(solve_ms) / 1e3
+    it_bytes = iteration_bytes(n, prob["K"].nnz, nnz_g, nnz_gt)
+
+    with open(ROOT / "MEASURED_PEAKS.json") as f:
+        peaks = json.load(f)
+    peak = float(peaks["hbm_gbs"])
+    achieved = it_bytes * total_iters / solve_total_s / 1e9
+
+    apply = measure_applies(pre, K, mass, free, n, dev)
+    traffic = read_traffic()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded jittered tet cube; P1 cotangent stiffness; lumped mass)",
+        "config": workload_config(args, prob),
+        "setup_ms": statistics.median(setup_ms), "solve_ms": statistics.median(solve_ms),
+        "iterations": iters[-1], "true_relres": relres,
+        "fsai_nnz": nnz_g,
+        "roofline": {
+            "bound": "hbm", "unit": "GB/s", "kernel": "PCG iteration (factored operator + FSAI "
+            "apply + fused updates), averaged over the timed solves",
+            "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+            "algorithmic_bytes_per_iteration": it_bytes,
+            "traffic": traffic,
+        },
+        "apply_gbps": apply,
+        "gpu_launches": launch_count(iters),
+    }
+    clk = clocks.summary()
+    line["clocks"] = clk
+    if not args.no_e2e:
+        line["e2e"] = run_e2e(args, prob, dev, one_step, world, dist)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline_sample(prob, args.width, args.step_size, args.method, args.cpu_iters,
+                                 iters[-1])
+        line["cpu_baseline"] = {
+            "value": 4.0 / cb["total_s"], "unit": "solves/s", "cores": cb["threads"],
+            "kind": "port",
+            "sample": (f"oracle FSAI w{args.width} setup ({cb['setup_s']:.2f} s) + "
+                       f"{cb['iters_sampled']} PCG iterations ({cb['per_iteration_s'] * 1e3:.2f} "
+                       f"ms each) on one RHS, extrapolated to the GPU's iteration counts "
+                       f"{iters[-1]}"),
+        }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def launch_count(iters):
+    """Kernels of ours launched per timed step, times steps (structure of the code):
+    setup = sqlap (index, mass, gather, boundary map, 3 x SELL build of 2 kernels + scan)
+    + FSAI (diag, prep, build, scan 3, pack, transpose 6, 2 x SELL build 3) ;
+    solve = init 7 + 6 per CG iteration."""
+    setup = 4 + 3 * 3 + 3 + 3 + 1 + 6 + 2 * 3
+    return sum(setup + sum(7 + 6 * i for i in step) for step in iters)
+
+
+def measure_applies(pre, K, mass, free, n, dev):
+    """Live CUDA-event timing of the two applies on the step's data (GB/s)."""
+    import torch
+
+    from warp_preconditioners_gb300 import SquaredLaplacianOperator
+
+    op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
+    x = torch.randn(n, dtype=torch.float64, device=dev)
+    z = torch.empty_like(x)
+    out = {}
+    for name, fn, nbytes in (
+        ("fsai_apply", lambda: pre.matvec(x, x, z, 1.0, 0.0),
+         (pre.G.nnz + pre.GT.nnz) * 12 + 2 * 4 * (n + 1) + 4 * n * 8),
+        ("factored_operator_apply", lambda: op.matvec(x, x, z, 1.0, 0.0),
+         2 * (K.nnz * 12 + 4 * (n + 1)) + 6 * n * 8),
+    ):
+        for _ in range(5):
+            fn()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        reps = 50
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        torch.cuda.synchronize()
+        t = s.elapsed_time(e) / reps / 1e3
+        out[name] = {"us": t * 1e6, "gbps": nbytes / t / 1e9, "bytes": nbytes}
+    return out
+
+
+def read_traffic():
+    """Measured DRAM bytes per PCG iteration from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "pcg_iteration_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_iteration:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def run_e2e(args, prob, dev, one_step, world, dist):
+    """Same metric from pinned host buffers through the public API."""
+    import torch
+
+    from warp_preconditioners_gb300.sparse import BsrMatrix
+
+    Qh, Kh = prob["Q"], prob["K"]
+
+    def pinned(a, dtype=None):
+        t = torch.as_tensor(np.ascontiguousarray(a))
+        if dtype is not None:
+            t = t.to(dtype)
+        return t.pin_memory()
+
+    host = {
+        "q_off": pinned(Qh.indptr.astype(np.int32)), "q_col": pinned(Qh.indices.astype(np.int32)),
+        "q_val": pinned(Qh.data), "k_off": pinned(Kh.indptr.astype(np.int32)),
+        "k_col": pinned(Kh.indices.astype(np.int32)), "k_val": pinned(Kh.data),
+        "mass": pinned(prob["mass"]), "rhs": pinned(prob["rhs"]),
+    }
+    out_host = torch.empty((4, prob["n"]), dtype=torch.float64).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = out_host.numel() * out_host.element_size()
+
+    def step():
+        d = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+        Qm = BsrMatrix(Qh.shape[0], Qh.shape[1], (1, 1), d["q_off"], d["q_col"], d["q_val"])
+        Km = BsrMatrix(Kh.shape[0], Kh.shape[1], (1, 1), d["k_off"], d["k_col"], d["k_val"])
+        xs = torch.empty((4, prob["n"]), dtype=torch.float64, device=dev)
+        one_step(Qm, Km, d["mass"], d["rhs"], xs)
+        out_host.copy_(xs, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.steps):
+        step()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return {"value": 4.0 * args.steps * world / (ms / 1e3), "unit": "solves/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": ms / args.steps}
+
+
+if __name__ == "__main__":
+    main()

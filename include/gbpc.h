@@ -1,0 +1,252 @@
+/*
+ * gbpc.h — C ABI of the GB300-native preconditioned-Krylov library (libgbpc.so).
+ *
+ * Drop-in boundary for the hot path of alecjacobson/warp-preconditioners:
+ * adaptive FSAI setup and application, cooperative sparse products, the
+ * factored squared-Laplacian (biharmonic) operator, block Jacobi, block
+ * ILU(0), block FSAI, scalar Jacobi, and the CG / CR loops that the reference
+ * runs through warp.optim.linear.
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer (cudaMalloc, torch, or any
+ *     allocator on the current device) unless its name ends in `_host`.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream).
+ *   - Index arrays are int32, CSR/BSR rows sorted with unique columns; BSR
+ *     blocks are b x b, row-major, stored contiguously per block.
+ *   - dtype codes: GBPC_F64, GBPC_F32, GBPC_BF16 (storage only).
+ *   - Every function returns 0 (GBPC_OK) or a positive GBPC_ERR_* code;
+ *     gbpc_last_error() gives a message for the calling thread.
+ *   - Setup entry points synchronise `stream` to read validation counters
+ *     (as the reference does); apply and solve entry points are
+ *     stream-ordered, never synchronise and never allocate.
+ *   - Linear operators follow the reference's LinearOperator.matvec contract
+ *     z = alpha * Op * x + beta * y: x, y, z may alias each other, beta == 0
+ *     never reads y and alpha == 0 never reads x.
+ *   - An operator owns scratch memory: do not apply one operator concurrently
+ *     on independent streams.
+ */
+#ifndef GBPC_H
+#define GBPC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum gbpc_status {
+  GBPC_OK = 0,
+  GBPC_ERR_ARG = 1,          /* invalid argument (message says which) */
+  GBPC_ERR_CUDA = 2,         /* CUDA runtime error */
+  GBPC_ERR_DIAGONAL = 3,     /* FSAI: non-finite or non-positive diagonal ("positive diagonals") */
+  GBPC_ERR_FACTOR = 4,       /* FSAI: factor lost finite entries or a positive diagonal */
+  GBPC_ERR_CONVERSION = 5,   /* FSAI: factor dtype conversion lost finite entries or a positive diagonal */
+  GBPC_ERR_PIVOT = 6,        /* block Jacobi / ILU(0): missing, non-finite or singular block pivot */
+  GBPC_ERR_FREE_INDEX = 7,   /* squared Laplacian: free indices not distinct or out of bounds */
+  GBPC_ERR_MASS = 8,         /* mass entries not finite and positive */
+  GBPC_ERR_TIMEOUT = 9,      /* a bounded device wait gave up */
+  GBPC_ERR_NOMEM = 10,       /* device allocation failed */
+  GBPC_ERR_UNSUPPORTED = 11, /* input outside what this build implements (message says what) */
+  GBPC_ERR_BLOCK_PIVOT = 12  /* block FSAI: non-positive local pivot */
+};
+
+enum gbpc_dtype { GBPC_F64 = 0, GBPC_F32 = 1, GBPC_BF16 = 2 };
+
+enum gbpc_method { GBPC_CG = 0, GBPC_CR = 1 };
+
+/* Message of the last failing call on this thread (never NULL). */
+const char* gbpc_last_error(void);
+/* ABI version, currently 1. */
+int gbpc_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* FSAI setup stages                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* Adaptive FSAI factor rows.  Replaces the `diagonal` and `build` kernels and
+ * their launches, warp_preconditioners/fsai.py:44-176 and :305-339, fused with
+ * `sort_rows` (warp_preconditioners/fsai_pack.py:15-39).
+ * Input: canonical scalar CSR A (n x n, dtype F64 or F32, arithmetic in that
+ * type), width = max_row_size in [1, 64], step = max_step_size in [1, 64].
+ * Output (device): ell_cols[n*width], ell_vals[n*width] (columns ascending,
+ * the diagonal last, unused slots -1 / 0), row_counts[n], scale[n] = a_ii^-1/2.
+ * status_host[3] receives the reference's counters: [0] invalid diagonals,
+ * [1] truncated rows (pivot guard), [2] rows that lost finiteness or a
+ * positive diagonal.  Returns GBPC_ERR_DIAGONAL / GBPC_ERR_FACTOR when the
+ * reference raises.  Synchronises `stream`. */
+int gbpc_fsai_setup(int n, const int32_t* offsets, const int32_t* columns, const void* values,
+                    int dtype, int width, int step, double kap_tolerance, double pivot_floor,
+                    int32_t* ell_cols, void* ell_vals, int32_t* row_counts, void* scale,
+                    int32_t* status_host, void* stream);
+
+/* Compact sorted ELL rows to CSR.  Replaces `array_scan` + `pack`
+ * (warp_preconditioners/fsai_pack.py:42-71).  With columns_out == NULL only
+ * offsets_out[n+1] is written and *nnz_host returned (synchronises); call
+ * again with the arrays sized *nnz_host. */
+int gbpc_fsai_pack(int n, int width, const int32_t* ell_cols, const void* ell_vals,
+                   const int32_t* row_counts, int dtype, int32_t* offsets_out,
+                   int32_t* columns_out, void* values_out, int64_t* nnz_host, void* stream);
+
+/* Explicit transpose of canonical CSR (rows of the result ascending).
+ * Replaces warp.sparse.bsr_transposed as called at
+ * warp_preconditioners/fsai.py:356.  t_off[ncol+1], t_col/t_val[nnz]. */
+int gbpc_csr_transpose(int nrow, int ncol, const int32_t* offsets, const int32_t* columns,
+                       const void* values, int dtype, int32_t* t_off, int32_t* t_col,
+                       void* t_val, void* stream);
+
+/* Canonical b x b BSR to scalar CSR keeping stored zeros.  Replaces
+ * `scalarize` / `scalarize_compact` (warp_preconditioners/fsai_pack.py:74-130).
+ * out_off[nrow_blocks*b+1], out_col/out_val[nnzb*b*b]. */
+int gbpc_scalarize(int nrow_blocks, int b, const int32_t* offsets, const int32_t* columns,
+                   const void* values, int dtype, int32_t* out_off, int32_t* out_col,
+                   void* out_val, void* stream);
+
+/* Factor storage conversion with validation.  Replaces the bsr_copy to a
+ * narrower scalar type and `_validate_float32_factor`
+ * (warp_preconditioners/fsai.py:181-196, :343-355).  *invalid_host receives
+ * the number of rows with a non-finite value or a non-positive diagonal;
+ * returns GBPC_ERR_CONVERSION when it is non-zero.  Synchronises. */
+int gbpc_convert_factor(int n, const int32_t* offsets, const int32_t* columns, const void* src,
+                        int src_dtype, void* dst, int dst_dtype, int32_t* invalid_host,
+                        void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Linear operators                                                          */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbpc_op gbpc_op;
+
+/* z = alpha * A x + beta * y for square-block BSR A (block 1..4; block 1 is
+ * scalar CSR).  Replaces SparseOperator (warp_preconditioners/
+ * sparse_operator.py:107-139), its `_matvec` dispatch (:90-104) and
+ * warp.sparse.bsr_mv for the A-apply of cg/cr.  value_dtype F64/F32/BF16;
+ * vector_dtype F64 or F32.  Copies A into a device SELL-32 layout. */
+int gbpc_op_sparse(int nrow, int ncol, int block, const int32_t* offsets,
+                   const int32_t* columns, const void* values, int value_dtype,
+                   int vector_dtype, void* stream, gbpc_op** out);
+
+/* Gram-form approximate inverse z = alpha * G^T (G x) + beta * y from
+ * explicit G and G^T (scalar CSR, or b x b BSR for block FSAI).  Replaces
+ * FSAI._apply (warp_preconditioners/fsai.py:393-400) and BsrBlockFSAI._apply
+ * (benchmarks/block_fsai_candidate.py:311-332). */
+int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int32_t* g_col,
+                 const void* g_val, const int32_t* gt_off, const int32_t* gt_col,
+                 const void* gt_val, int value_dtype, int vector_dtype, void* stream,
+                 gbpc_op** out);
+
+/* Factored (L diag(1/mass) L + mass_weight diag(mass))[free, free].
+ * Replaces SquaredLaplacianOperator (warp_preconditioners/
+ * squared_laplacian.py:103-198): setup `_index_free` + `mass_inverse`,
+ * apply `forward` + `backward`.  L: scalar CSR n x n (F64 or F32),
+ * mass[n], free[nfree].  Returns GBPC_ERR_FREE_INDEX / GBPC_ERR_MASS
+ * as the reference raises.  Synchronises. */
+int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* columns, const void* values,
+                  int dtype, const void* mass, const int32_t* free_indices, int nfree,
+                  double mass_weight, void* stream, gbpc_op** out);
+
+/* Eliminated right-hand side -((L M^-1 L) u_b)[free] of
+ * SquaredLaplacianOperator.rhs (warp_preconditioners/squared_laplacian.py:
+ * 200-218).  boundary_values[n], out[nfree]. */
+int gbpc_sqlap_rhs(gbpc_op* op, const void* boundary_values, void* out, void* stream);
+
+/* Scalar Jacobi z = alpha * x / diag(A) + beta * y on the scalar diagonal of
+ * a BSR matrix.  Replaces warp.optim.linear.preconditioner(A, "diag") as used
+ * at benchmarks/block_challenge.py:259-261 and benchmarks/synthetic.py:37. */
+int gbpc_op_diagonal(int nrow, int block, const int32_t* offsets, const int32_t* columns,
+                     const void* values, int dtype, void* stream, gbpc_op** out);
+
+/* Block Jacobi: inverse diagonal blocks (1..4) with the scaled-determinant
+ * guard.  Replaces BlockJacobi (warp_preconditioners/block_ilu.py:225-345):
+ * `diagonal_only` + `safe_inverse` (:17-43, :76-104), `diagonal_apply`
+ * (:188-202).  inverse_out[nrow*b*b] (optional, may be NULL) receives the
+ * inverse blocks.  Returns GBPC_ERR_PIVOT when a pivot is missing, non-finite
+ * or singular.  Synchronises. */
+int gbpc_op_block_jacobi(int nrow, int block, const int32_t* offsets, const int32_t* columns,
+                         const void* values, int dtype, double pivot_tolerance,
+                         void* inverse_out, void* stream, gbpc_op** out);
+
+/* Synchronous block ILU(0) with Jacobi triangular sweeps.  Replaces BlockILU0
+ * (warp_preconditioners/block_ilu.py:347-450): `topology`, `invert`,
+ * `initialize`, `sweep`, `validate_factors` for setup and `triangular` +
+ * `combine` for apply.  factors_out[nnzb*b*b] and inverse_out[nrow*b*b]
+ * optional.  Synchronises. */
+int gbpc_op_bilu0(int nrow, int block, const int32_t* offsets, const int32_t* columns,
+                  const void* values, int dtype, int factor_sweeps, int solve_sweeps,
+                  double relaxation, double pivot_tolerance, void* factors_out,
+                  void* inverse_out, void* stream, gbpc_op** out);
+
+/* Block-row adaptive FSAI rows (benchmarks/block_fsai_candidate.py:45-178,
+ * `diagonal` + `build`): input b x b BSR (F64, b in 2..4, b*max_blocks <= 16),
+ * output scalar ELL rows of width b*max_blocks (ell_cols/ell_vals
+ * [nrow*b*b*max_blocks]), sorted by column like fsai_pack.py:15-39, with
+ * row_counts[nrow*b], and scale[nrow*b].  refit != 0 reuses the supports
+ * already in ell_cols.  Returns GBPC_ERR_BLOCK_PIVOT on a non-positive local
+ * pivot.  Synchronises. */
+int gbpc_block_fsai_setup(int nrow, int block, int max_blocks, const int32_t* offsets,
+                          const int32_t* columns, const void* values, int refit,
+                          int32_t* ell_cols, void* ell_vals, int32_t* row_counts, void* scale,
+                          void* stream);
+
+/* Scalar CSR whose rows come in groups of `block` to b x b BSR, zero-filling
+ * missing entries of a stored block.  Replaces warp.sparse.bsr_copy(G,
+ * block_shape=(b, b)) at benchmarks/block_fsai_candidate.py:300.  With
+ * b_col == NULL only b_off[nrow_blocks+1] and *nnzb_host are produced
+ * (synchronises); call again with b_col[nnzb], b_val[nnzb*b*b]. */
+int gbpc_csr_to_bsr(int nrow_blocks, int block, const int32_t* offsets, const int32_t* columns,
+                    const void* values, int dtype, int32_t* b_off, int32_t* b_col, void* b_val,
+                    int64_t* nnzb_host, void* stream);
+
+/* Explicit transpose of b x b BSR, transposing every block.  Replaces
+ * warp.sparse.bsr_transposed at benchmarks/block_fsai_candidate.py:301 and
+ * warp_preconditioners/biharmonic.py:98.  Synchronises. */
+int gbpc_bsr_transpose(int nrow, int ncol, int block, const int32_t* offsets,
+                       const int32_t* columns, const void* values, int dtype, int32_t* t_off,
+                       int32_t* t_col, void* t_val, void* stream);
+
+/* Apply an operator: z = alpha * Op * x + beta * y (vectors of the
+ * operator's vector dtype, length = scalar rows).  Stream-ordered. */
+int gbpc_op_apply(gbpc_op* op, const void* x, const void* y, void* z, double alpha, double beta,
+                  void* stream);
+
+/* Scalar length of the operator's vectors. */
+int gbpc_op_rows(const gbpc_op* op, int64_t* rows_host);
+
+/* Release an operator and its device memory (synchronises the device). */
+int gbpc_op_destroy(gbpc_op* op);
+
+/* ------------------------------------------------------------------------ */
+/* Krylov solvers                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* Preconditioned CG (method GBPC_CG) or CR (GBPC_CR) on float64 vectors,
+ * replacing warp.optim.linear.cg / cr as called at
+ * benchmarks/block_challenge.py:131-139 and visualization/solve_fields.py:
+ * 121-124.  Stops when the recursive r.r <= max(atol, tol |b|)^2 or after
+ * maxiter iterations (maxiter <= 0 means n).  The whole loop runs on the
+ * device inside one CUDA graph with a conditional while-node (use_graph != 0)
+ * or as a host loop of the same kernels (use_graph == 0).  M may be NULL.
+ * Device outputs (any may be NULL): nit_dev[1] int32, rr_dev[1] and
+ * atol_sq_dev[1] float64 — stream-ordered, no synchronisation.  When any
+ * *_host output is non-NULL the call synchronises and fills it. */
+int gbpc_krylov(int method, gbpc_op* A, gbpc_op* M, const double* b, double* x, double tol,
+                double atol, int maxiter, int use_graph, int32_t* nit_dev, double* rr_dev,
+                double* atol_sq_dev, int32_t* nit_host, double* rr_host, double* atol_sq_host,
+                void* stream);
+
+/* Reusable solver: owns the work vectors and a cached CUDA graph for the
+ * last (b, x) pair, so repeated solves cost one graph launch each.
+ * gbpc_solver_run is stream-ordered and never synchronises; outputs as for
+ * gbpc_krylov.  Same reference call sites as gbpc_krylov. */
+typedef struct gbpc_solver gbpc_solver;
+int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_graph, void* stream,
+                       gbpc_solver** out);
+int gbpc_solver_run(gbpc_solver* solver, const double* b, double* x, double tol, double atol,
+                    int maxiter, int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
+                    void* stream);
+int gbpc_solver_destroy(gbpc_solver* solver);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPC_H */

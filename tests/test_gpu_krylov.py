@@ -1,0 +1,118 @@
+"""CG / CR on the GPU: convergence, device-array returns, agreement with the
+oracle's PCG / PCR, and the end-to-end solves of the benchmark shapes."""
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_helpers import cuda, oracle_csr, to_bsr, vec
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("method", ["cg", "cr"])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_fsai_krylov_matches_oracle(oracle, method, use_graph):
+    from warp_preconditioners_gb300 import FSAI, linear, problems
+
+    a = problems.laplacian_2d(64)
+    A = to_bsr(a)
+    pre = FSAI(A, max_row_size=8)
+    b_np = problems.uniform_rhs(a.shape[0], 0)
+    b = vec(b_np)
+    x = torch.zeros_like(b)
+    solve = linear.cg if method == "cg" else linear.cr
+    nit, rr, atol_sq = solve(A, b, x, tol=1e-8, M=pre, maxiter=2000, check_every=0,
+                             use_cuda_graph=use_graph)
+    assert nit.dtype == torch.int32 and nit.is_cuda and rr.is_cuda
+    nit, rr, atol_sq = int(nit.item()), float(rr.item()), float(atol_sq.item())
+    assert rr <= atol_sq
+    sol = x.cpu().numpy()
+    assert np.linalg.norm(b_np - a @ sol) <= 1.01e-8 * np.linalg.norm(b_np)
+    g, gt, _ = oracle.fsai(oracle_csr(oracle, a), width=8)
+    x_or, it_or, rr_or, _ = oracle.krylov(method, oracle.Operator.csr(oracle_csr(oracle, a)), b_np,
+                                          M=oracle.Operator.fsai(g, gt), tol=1e-8, maxiter=2000)
+    # Same recurrence in different summation orders: iteration counts agree to
+    # within a couple of steps and both reach the tolerance.
+    assert abs(nit - it_or) <= 2
+    np.testing.assert_allclose(sol, x_or, rtol=1e-6, atol=1e-8 * np.abs(x_or).max())
+
+
+def test_host_return_values_and_maxiter():
+    from warp_preconditioners_gb300 import FSAI, linear, problems
+
+    a = problems.laplacian_2d(32)
+    A = to_bsr(a)
+    b = vec(problems.uniform_rhs(a.shape[0], 1))
+    x = torch.zeros_like(b)
+    it, res, atol = linear.cg(A, b, x, tol=1e-12, maxiter=7, M=FSAI(A))
+    assert it == 7 and res > atol
+    x.zero_()
+    it, res, atol = linear.cg(A, b, x, tol=1e-6, maxiter=1000, M=linear.preconditioner(A, "diag"))
+    assert res <= atol and 0 < it < 1000
+    np.testing.assert_allclose(atol, 1e-6 * np.linalg.norm(b.cpu().numpy()), rtol=1e-12)
+    # Already converged: zero iterations, x untouched.
+    it, res, atol = linear.cg(A, b, x, tol=1e-6, maxiter=1000)
+    assert it == 0
+
+
+@pytest.mark.parametrize("method", ["cg", "cr"])
+def test_unconstrained_smoothing_matches_direct_solve(method):
+    # tests/test_squared_laplacian.py:111-136
+    import scipy.sparse as ss
+    import scipy.sparse.linalg as sla
+
+    from warp_preconditioners_gb300 import SquaredLaplacianOperator, linear
+
+    n = 23
+    lap = ss.diags([-np.ones(n - 1), np.r_[1.0, np.full(n - 2, 2.0), 1.0], -np.ones(n - 1)],
+                   [-1, 0, 1]).tocsr()
+    mass = np.linspace(0.5, 2.0, n)
+    target = np.sin(np.arange(n))
+    weight = 0.03
+    expected_matrix = lap @ ss.diags(1 / mass) @ lap + ss.diags(weight * mass)
+    op = SquaredLaplacianOperator(to_bsr(lap), vec(mass),
+                                  torch.arange(n, dtype=torch.int32, device=cuda()), row_lanes=4,
+                                  mass_weight=weight)
+    rhs = vec(weight * mass * target)
+    x = vec(target)
+    getattr(linear, method)(op, rhs, x, tol=1e-12, maxiter=300)
+    np.testing.assert_allclose(x.cpu().numpy(), sla.spsolve(expected_matrix, weight * mass * target),
+                               rtol=1e-10, atol=1e-11)
+
+
+def test_block_jacobi_and_ilu_solve_coupling():
+    from warp_preconditioners_gb300 import BlockILU0, BlockJacobi, linear, problems
+
+    bsr, _ = problems.kron_coupling(10, 1e-6)
+    A = to_bsr(bsr.toarray(), block=3)
+    b_np = problems.uniform_rhs(bsr.shape[0], 0)
+    for pre in (BlockJacobi(A, pivot_tolerance=1e-15), BlockILU0(A, 3, 3, pivot_tolerance=1e-15)):
+        for solve in (linear.cg, linear.cr):
+            x = torch.zeros(bsr.shape[0], dtype=torch.float64, device=cuda())
+            it, res, atol = solve(A, vec(b_np), x, tol=1e-8, maxiter=5000, M=pre)
+            assert res <= atol, (type(pre).__name__, solve.__name__, it, res, atol)
+            rel = np.linalg.norm(b_np - bsr @ x.cpu().numpy()) / np.linalg.norm(b_np)
+            assert rel < 1e-6
+
+
+def test_biharmonic_tet_cube_solve(oracle):
+    # The smoothing configuration on a small cube, all four right-hand sides.
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, linear, problems
+
+    verts, _, K, mass = problems.tet_cube(12)
+    alpha = 1e-4
+    q = problems.biharmonic(K, mass, alpha)
+    n = K.shape[0]
+    op = SquaredLaplacianOperator(to_bsr(K), vec(mass),
+                                  torch.arange(n, dtype=torch.int32, device=cuda()),
+                                  mass_weight=alpha)
+    pre = FSAI(to_bsr(q), max_row_size=8)
+    rhs = problems.smoothing_rhs(verts, mass, alpha)
+    solver = linear.Solver("cg", op, pre)
+    for k in range(4):
+        x = torch.zeros(n, dtype=torch.float64, device=cuda())
+        nit, rr, atol_sq = solver.run(vec(rhs[k]), x, tol=1e-8, maxiter=20000)
+        assert rr.item() <= atol_sq.item()
+        sol = x.cpu().numpy()
+        assert np.linalg.norm(rhs[k] - q @ sol) <= 1e-7 * np.linalg.norm(rhs[k])

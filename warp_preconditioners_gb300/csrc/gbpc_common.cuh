@@ -1,0 +1,224 @@
+// Shared device-side definitions for the GB300 preconditioned-Krylov library.
+//
+// Storage formats
+//   * CSR / BSR: the reference's canonical compact layout (sorted, unique
+//     column indices per row; b x b blocks stored row-major).
+//   * SELL-32: "sliced ELL" with 32 (block) rows per slice, stored
+//     column-major inside each slice so that the 32 lanes of a warp read 32
+//     consecutive words.  Padding slots carry column -1 and are skipped, so a
+//     NaN in x behind a padding slot never leaks into a row sum.
+//
+// Arithmetic notes for GB300 (sm_103a): FP64 issues at 1/64 of the FP32 rate
+// and an FP64 warp instruction costs the same whether 1 or 32 lanes are
+// active, so FP64 kernels keep all lanes busy (one row per thread) and keep
+// reductions short.  Reductions are deterministic: per-CTA partials summed in
+// a fixed order by the last CTA to finish.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "../../include/gbpc.h"
+
+namespace gbpc {
+
+constexpr int kSlice = 32;     // rows per SELL slice (one warp)
+constexpr int kThreads = 256;  // threads per CTA for streaming kernels
+
+// ---------------------------------------------------------------------------
+// Value conversion helpers.
+
+template <typename T> __device__ __forceinline__ double to_double(T v) { return (double)v; }
+template <> __device__ __forceinline__ double to_double<__nv_bfloat16>(__nv_bfloat16 v) {
+  return (double)__bfloat162float(v);
+}
+template <typename T> __device__ __forceinline__ float to_float(T v) { return (float)v; }
+template <> __device__ __forceinline__ float to_float<__nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+template <typename A, typename S> __device__ __forceinline__ A widen(S v);
+template <> __device__ __forceinline__ double widen<double, double>(double v) { return v; }
+template <> __device__ __forceinline__ double widen<double, float>(float v) { return (double)v; }
+template <> __device__ __forceinline__ double widen<double, __nv_bfloat16>(__nv_bfloat16 v) {
+  return (double)__bfloat162float(v);
+}
+template <> __device__ __forceinline__ float widen<float, float>(float v) { return v; }
+template <> __device__ __forceinline__ float widen<float, __nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+template <> __device__ __forceinline__ float widen<float, double>(double v) { return (float)v; }
+
+// ---------------------------------------------------------------------------
+// SELL-32 view (device pointers).  Slice s covers block rows [32 s, 32 s + 32)
+// and entries [slice_ptr[s], slice_ptr[s+1]); entry (k, lane) of slice s is at
+// E = slice_ptr[s] + 32 k + lane.  Its column is cols[E]; component q of its
+// B x B block is vals[slice_ptr[s] * B * B + (k * B * B + q) * 32 + lane].
+template <typename V>
+struct SellView {
+  int nrow;        // block rows
+  int nslices;
+  const int64_t* slice_ptr;
+  const int32_t* cols;
+  const V* vals;
+};
+
+// ---------------------------------------------------------------------------
+// Krylov scalars, resident on the device for the whole solve.
+struct KrylovScalars {
+  double bb;       // b.b
+  double atol_sq;  // max(atol, tol |b|)^2
+  double rr;       // recursive r.r
+  double rz;       // CG: r.z   | CR: z.Az
+  double rz_new;
+  double denom;    // CG: p.Ap  | CR: y.Ap
+  double alpha;
+  double beta;
+  int it;
+  int maxiter;
+  int active;
+  int pad;
+  unsigned long long cond_handle;  // cudaGraphConditionalHandle (0 = none)
+  double tol;
+  double atol;
+};
+
+// What the last CTA does with a finished reduction.
+enum FinMode : int {
+  FIN_NONE = 0,
+  FIN_STORE = 1,       // *out = total
+  FIN_INIT_BB = 2,     // bb = total
+  FIN_INIT_RR = 3,     // rr = total; atol_sq; active; graph condition
+  FIN_CG_ALPHA = 4,    // denom = total; alpha = rz / denom
+  FIN_RR = 5,          // rr = total
+  FIN_CG_BETA = 6,     // beta = total / rz; rz = total; it++; active
+  FIN_INIT_RZ = 7,     // rz = total
+  FIN_CR_ALPHA = 8,    // denom = total; alpha = rz / denom  (rz holds z.Az)
+};
+
+struct Reduction {
+  const double* w;         // dot(w, out) with the kernel's output (nullptr: no dot)
+  double* partials;        // per-CTA partial sums (>= gridDim.x entries)
+  unsigned int* counter;   // arrival counter, zero between uses
+  int mode;                // FinMode
+  KrylovScalars* ks;
+  double* out;             // FIN_STORE destination
+};
+
+__device__ __forceinline__ bool guard_off(const int* guard) {
+  return guard != nullptr && *(volatile const int*)guard == 0;
+}
+
+// Sum of one double per thread over a CTA of kThreads threads with few FP64
+// instructions: transpose through shared memory so warp 0 adds 8 values per
+// lane with full lanes, then a 5-step shuffle tree.  Result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v, double* smem /*kThreads*/) {
+  smem[threadIdx.x] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x < 32) {
+    s = smem[threadIdx.x];
+#pragma unroll
+    for (int k = 1; k < kThreads / 32; ++k) s += smem[threadIdx.x + 32 * k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  }
+  __syncthreads();
+  return s;
+}
+
+// Krylov bookkeeping done by one thread once a reduction is complete.  The
+// stopping rule mirrors warp.optim.linear: continue while r.r > atol^2 and
+// fewer than maxiter iterations have run.
+__device__ __forceinline__ void set_active(KrylovScalars* ks) {
+  const int active = (ks->rr > ks->atol_sq) && (ks->it < ks->maxiter);
+  ks->active = active;
+  if (ks->cond_handle != 0ull)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)ks->cond_handle, active ? 1u : 0u);
+}
+
+__device__ __forceinline__ void finalize(const Reduction& red, double total) {
+  KrylovScalars* ks = red.ks;
+  switch (red.mode) {
+    case FIN_STORE:
+      *red.out = total;
+      break;
+    case FIN_INIT_BB:
+      ks->bb = total;
+      break;
+    case FIN_INIT_RR: {
+      ks->rr = total;
+      const double a = fmax(ks->atol, ks->tol * sqrt(ks->bb));
+      ks->atol_sq = a * a;
+      ks->it = 0;
+      set_active(ks);
+      break;
+    }
+    case FIN_INIT_RZ:
+      ks->rz = total;
+      break;
+    case FIN_CG_ALPHA:
+    case FIN_CR_ALPHA:
+      ks->denom = total;
+      ks->alpha = ks->rz / total;
+      break;
+    case FIN_RR:
+      ks->rr = total;
+      break;
+    case FIN_CG_BETA:
+      ks->rz_new = total;
+      ks->beta = total / ks->rz;
+      ks->rz = total;
+      ks->it += 1;
+      set_active(ks);
+      break;
+    default:
+      break;
+  }
+}
+
+// Every thread of the CTA calls this with its partial; the last CTA to arrive
+// sums all CTA partials in index order and applies the finalize action.
+__device__ __forceinline__ void reduce_and_finalize(const Reduction& red, double v) {
+  __shared__ double smem[kThreads];
+  __shared__ bool am_last;
+  const double s = block_sum(v, smem);
+  if (threadIdx.x == 0) {
+    red.partials[blockIdx.x] = s;
+    __threadfence();
+    const unsigned int t = atomicAdd(red.counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    double acc = 0.0;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += kThreads) acc += __ldcg(red.partials + k);
+    const double total = block_sum(acc, smem);
+    if (threadIdx.x == 0) {
+      *red.counter = 0u;
+      finalize(red, total);
+    }
+  }
+}
+
+inline int grid_for(int64_t items, int per_cta) {
+  int64_t g = (items + per_cta - 1) / per_cta;
+  if (g < 1) g = 1;
+  if (g > 0x7fffffff) g = 0x7fffffff;
+  return (int)g;
+}
+
+}  // namespace gbpc
+
+#define GBPC_CUDA_TRY(expr)                         \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) {                        \
+      gbpc_set_error_cuda(_e, #expr, __FILE__, __LINE__); \
+      return GBPC_ERR_CUDA;                         \
+    }                                               \
+  } while (0)
+
+void gbpc_set_error(const char* fmt, ...);
+void gbpc_set_error_cuda(cudaError_t e, const char* expr, const char* file, int line);

@@ -1,0 +1,875 @@
+// Adaptive FSAI setup on GB300: one warp per factor row.
+//
+// Follows warp_preconditioners/fsai.py:44-176 operation for operation so that
+// the selected supports and the factor values are bit-identical to a
+// non-contracting evaluation of the reference (this file is compiled with
+// -fmad=false; every product and sum is rounded separately, divisions and
+// square roots are IEEE-exact).
+//
+// What differs from the reference is the work distribution, not arithmetic:
+//   * candidate scores are accumulated by walking the rows of the current
+//     support in support order (q = 0, 1, ...), reading the transposed entry
+//     A[c, S_q] through a precomputed transpose position, into a per-warp
+//     shared-memory hash table keyed by column.  Each candidate's residual is
+//     therefore summed in exactly the reference's order (absent terms are
+//     exact zeros and are skipped), but without one binary search per term;
+//   * equilibrated entries (a_ij * s_i) * s_j are computed once per nonzero;
+//   * the top-`step` selection is a warp-wide arg-max on the IEEE bit pattern
+//     of |residual| (non-negative doubles order like their bit patterns), with
+//     the reference's tie-break (higher score, then lower column);
+//   * the bordered Cholesky forward solve runs column-oriented across lanes,
+//     which performs the same subtraction sequence per entry as the
+//     reference's row-oriented loop.
+// The transpose-position lookup needs a structurally symmetric matrix (any
+// SPD input assembled by summation is); other inputs are rejected.
+
+#include <algorithm>
+#include <vector>
+
+#include "gbpc_common.cuh"
+#include "gbpc_internal.h"
+
+namespace gbpc {
+
+namespace {
+
+constexpr int kEmpty = -1;
+constexpr int kTomb = -2;
+
+template <typename T> struct Bits;
+template <> struct Bits<double> {
+  using U = unsigned long long;
+  static __device__ __forceinline__ U abs_bits(double v) {
+    return (U)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  }
+  static constexpr U kInf = 0x7ff0000000000000ull;
+};
+template <> struct Bits<float> {
+  using U = unsigned int;
+  static __device__ __forceinline__ U abs_bits(float v) { return (U)__float_as_uint(v) & 0x7fffffffu; }
+  static constexpr U kInf = 0x7f800000u;
+};
+
+__device__ __forceinline__ unsigned int hash_col(int c) { return (unsigned int)c * 2654435761u; }
+
+__device__ __forceinline__ int lower_bound_row(const int32_t* col, int lo, int hi, int j) {
+  while (lo < hi) {
+    const int mid = (lo + hi) / 2;
+    if (col[mid] < j) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// fsai.py:44-57: s_i = 1/sqrt(a_ii) or a counted failure.
+template <typename T>
+__global__ void fsai_diag_kernel(int n, const int32_t* __restrict__ off,
+                                 const int32_t* __restrict__ col, const T* __restrict__ val,
+                                 T* scale, int32_t* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int lo = lower_bound_row(col, off[i], off[i + 1], i);
+  T d = T(0);
+  if (lo < off[i + 1] && col[lo] == i) d = val[lo];
+  if (d > T(0) && isfinite(d)) {
+    scale[i] = T(1) / sqrt(d);
+  } else {
+    scale[i] = T(0);
+    atomicAdd(status + 0, 1);
+  }
+}
+
+// Equilibrated entries and transposed equilibrated entries:
+//   ahat[e]  = (a_ij * s_i) * s_j            for e = (i, j)
+//   ahatT[e] = (a_ji * s_j) * s_i            (the entry (j, i) seen from row i)
+// status[3] counts entries without a stored transpose; status[4] is the
+// longest row.
+template <typename T>
+__global__ void fsai_prep_kernel(int n, const int32_t* __restrict__ off,
+                                 const int32_t* __restrict__ col, const T* __restrict__ val,
+                                 const T* __restrict__ scale, T* ahat, T* ahatT, int32_t* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int b = off[i], e_end = off[i + 1];
+  atomicMax(status + 4, e_end - b);
+  const T si = scale[i];
+  int missing = 0;
+  for (int e = b; e < e_end; ++e) {
+    const int j = col[e];
+    const T sj = scale[j];
+    const T t = val[e] * si;
+    ahat[e] = t * sj;
+    const int t_pos = lower_bound_row(col, off[j], off[j + 1], i);
+    if (t_pos < off[j + 1] && col[t_pos] == i) {
+      const T u = val[t_pos] * sj;
+      ahatT[e] = u * si;
+    } else {
+      ahatT[e] = T(0);
+      ++missing;
+    }
+  }
+  if (missing) atomicAdd(status + 3, missing);
+}
+
+struct BuildParams {
+  int n;
+  int width;      // W <= 64
+  int step;       // S <= 64
+  int hsize;      // candidate table slots (power of 2)
+  int hbits;
+  int psize;      // pattern table slots (power of 2, >= 2W)
+  int pbits;
+  const int32_t* rows;   // optional row list (fallback pass)
+  int nrows_list;
+  int32_t* overflow_list;
+  int32_t* overflow_count;
+};
+
+// Bytes of one warp's shared-memory slice, rounded to 16 so that every
+// warp's floating-point arrays start 16-byte aligned.
+template <typename T>
+__host__ __device__ constexpr size_t warp_smem_bytes(int W, int S, int H, int PH) {
+  return (sizeof(T) * ((size_t)W * (W + 1) / 2 + 4 * (size_t)W + (size_t)H) +
+          sizeof(int) * ((size_t)W + 2 * (size_t)PH + (size_t)H + (size_t)S) + 15) &
+         ~(size_t)15;
+}
+
+__device__ __forceinline__ int plookup(const int* pkey, const int* ppos, int pmask, int pbits, int c) {
+  unsigned int s = hash_col(c) >> (32 - pbits);
+  for (int probe = 0; probe <= pmask; ++probe) {
+    const int k = pkey[s];
+    if (k == c) return ppos[s];
+    if (k == kEmpty) return -1;
+    s = (s + 1) & pmask;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void pinsert(int* pkey, int* ppos, int pmask, int pbits, int c, int pos) {
+  unsigned int s = hash_col(c) >> (32 - pbits);
+  for (int probe = 0; probe <= pmask; ++probe) {
+    if (pkey[s] == kEmpty) {
+      pkey[s] = c;
+      ppos[s] = pos;
+      return;
+    }
+    s = (s + 1) & pmask;
+  }
+}
+
+// Find or insert column c in the candidate table; -1 when the table is full.
+__device__ __forceinline__ int hfind_insert(int* hkey, int hmask, int hbits, int c) {
+  unsigned int s = hash_col(c) >> (32 - hbits);
+  for (int probe = 0; probe <= hmask; ++probe) {
+    int k = hkey[s];
+    if (k == c) return (int)s;
+    if (k == kEmpty) {
+      k = atomicCAS(hkey + s, kEmpty, c);
+      if (k == kEmpty || k == c) return (int)s;
+    }
+    s = (s + 1) & hmask;
+  }
+  return -1;
+}
+
+// fsai.py:60-176, one warp per row (see the file comment).
+template <typename T>
+__global__ void __launch_bounds__(256)
+fsai_build_kernel(BuildParams P, const int32_t* __restrict__ off, const int32_t* __restrict__ col,
+                  const T* __restrict__ ahat, const T* __restrict__ ahatT,
+                  const T* __restrict__ scale, T tolerance, T pivot_floor, int32_t* ell_cols,
+                  T* ell_vals, int32_t* row_counts, int32_t* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using BitsT = Bits<T>;
+  using U = typename BitsT::U;
+  const int W = P.width, S = P.step, H = P.hsize, PH = P.psize;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + warp;
+  const int total = P.rows ? P.nrows_list : P.n;
+  if (gw >= total) return;
+  const int i = P.rows ? P.rows[gw] : gw;
+
+  unsigned char* base = smem_raw + (size_t)warp * warp_smem_bytes<T>(W, S, H, PH);
+  T* chol = reinterpret_cast<T*>(base);          // column-major packed lower triangle
+  T* z = chol + (size_t)W * (W + 1) / 2;
+  T* v = z + W;
+  T* a = v + W;
+  T* wv = a + W;
+  T* hacc = wv + W;
+  int* pattern = reinterpret_cast<int*>(hacc + H);
+  int* pkey = pattern + W;
+  int* ppos = pkey + PH;
+  int* hkey = ppos + PH;
+  int* cand = hkey + H;
+  const int hmask = H - 1, pmask = PH - 1;
+  // Column p of L starts at cs(p) = p*W - p*(p-1)/2 and holds rows p..W-1.
+  auto L = [&](int r, int p) -> T& { return chol[p * W - (p * (p - 1)) / 2 + (r - p)]; };
+
+  for (int s = lane; s < PH; s += 32) pkey[s] = kEmpty;
+  for (int s = lane; s < H; s += 32) hkey[s] = kEmpty;
+  __syncwarp();
+  if (lane == 0) {
+    pattern[0] = i;
+    pinsert(pkey, ppos, pmask, P.pbits, i, 0);
+    L(0, 0) = T(1);
+    z[0] = T(1);
+    v[0] = T(1);
+  }
+  __syncwarp();
+  int size = 1;
+  bool stopped = false;
+  bool truncated = false;
+  while (size < W) {
+    // Candidate residuals, summed in support order.
+    for (int s = lane; s < H; s += 32) hacc[s] = T(0);
+    __syncwarp();
+    bool overflow = false;
+    for (int q = 0; q < size; ++q) {
+      const int pq = pattern[q];
+      const T zq = z[q];
+      const int e_end = off[pq + 1];
+      for (int e = off[pq] + lane; e < e_end; e += 32) {
+        const int c = col[e];
+        if (c < i && plookup(pkey, ppos, pmask, P.pbits, c) < 0) {
+          const int slot = hfind_insert(hkey, hmask, P.hbits, c);
+          if (slot < 0) {
+            overflow = true;
+          } else {
+            const T t = ahatT[e] * zq;
+            hacc[slot] = hacc[slot] + t;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (__any_sync(0xffffffffu, overflow)) {
+      if (lane == 0) {
+        const int k = atomicAdd(P.overflow_count, 1);
+        P.overflow_list[k] = i;
+      }
+      return;
+    }
+    // Top-`step` distinct candidates: higher score, then lower column.
+    int nsel = 0;
+    for (int r = 0; r < S; ++r) {
+      U best_bits = 0;
+      int best_col = 0x7fffffff;
+      int best_slot = -1;
+      for (int s = lane; s < H; s += 32) {
+        const int k = hkey[s];
+        if (k < 0) continue;
+        const U bits = BitsT::abs_bits(hacc[s]);
+        if (bits == 0 || bits > BitsT::kInf) continue;  // zero or NaN: never selected
+        if (bits > best_bits || (bits == best_bits && k < best_col)) {
+          best_bits = bits;
+          best_col = k;
+          best_slot = s;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const U ob = __shfl_xor_sync(0xffffffffu, best_bits, o);
+        const int oc = __shfl_xor_sync(0xffffffffu, best_col, o);
+        const int os = __shfl_xor_sync(0xffffffffu, best_slot, o);
+        if (ob > best_bits || (ob == best_bits && oc < best_col)) {
+          best_bits = ob;
+          best_col = oc;
+          best_slot = os;
+        }
+      }
+      if (best_slot < 0) break;
+      if (lane == 0) {
+        cand[r] = best_col;
+        hkey[best_slot] = kTomb;
+      }
+      __syncwarp();
+      ++nsel;
+    }
+    if (nsel == 0) break;
+    const T old_z0 = z[0];
+    for (int r = 0; r < nsel; ++r) {
+      if (size == W) break;
+      const int best = cand[r];
+      // a[p] = (A[best, S_p] * s_best) * s_{S_p}, zero when not stored.
+      for (int p = lane; p < size; p += 32) a[p] = T(0);
+      __syncwarp();
+      {
+        const int e_end = off[best + 1];
+        for (int e = off[best] + lane; e < e_end; e += 32) {
+          const int pos = plookup(pkey, ppos, pmask, P.pbits, col[e]);
+          if (pos >= 0 && pos < size) a[pos] = ahat[e];
+        }
+      }
+      __syncwarp();
+      T a0 = (lane < size) ? a[lane] : T(0);
+      T a1 = (lane + 32 < size) ? a[lane + 32] : T(0);
+      T pivot = T(1);
+      T rhs = T(0);
+      for (int p = 0; p < size; ++p) {
+        const int owner = p & 31;
+        T wl = T(0);
+        if (lane == owner) wl = ((p < 32) ? a0 : a1) / L(p, p);
+        const T wp = __shfl_sync(0xffffffffu, wl, owner);
+        if (lane == 0) wv[p] = wp;
+        const T sq = wp * wp;
+        pivot = pivot - sq;
+        const T pr = wp * v[p];
+        rhs = rhs - pr;
+        if (lane > p && lane < size) {
+          const T t = L(lane, p) * wp;
+          a0 = a0 - t;
+        }
+        if (lane + 32 > p && lane + 32 < size) {
+          const T t = L(lane + 32, p) * wp;
+          a1 = a1 - t;
+        }
+      }
+      __syncwarp();
+      if (pivot <= pivot_floor || !isfinite(pivot)) {
+        truncated = true;
+        stopped = true;
+        break;
+      }
+      for (int p = lane; p < size; p += 32) L(size, p) = wv[p];
+      if (lane == 0) {
+        pattern[size] = best;
+        pinsert(pkey, ppos, pmask, P.pbits, best, size);
+        const T d = sqrt(pivot);
+        L(size, size) = d;
+        v[size] = rhs / d;
+      }
+      __syncwarp();
+      ++size;
+    }
+    // L^T z = v, in the reference's order.
+    if (lane == 0) {
+      for (int rev = 0; rev < size; ++rev) {
+        const int p = size - 1 - rev;
+        T acc = v[p];
+        for (int q = p + 1; q < size; ++q) {
+          const T t = L(q, p) * z[q];
+          acc = acc - t;
+        }
+        z[p] = acc / L(p, p);
+      }
+    }
+    __syncwarp();
+    if (stopped) break;
+    if (tolerance > T(0)) {
+      const T ratio = old_z0 / z[0];
+      if (T(1) - ratio <= tolerance) break;
+    }
+  }
+  // Normalise, validate, sort by column, write the ELL row.
+  const T norm = sqrt(z[0]);
+  bool valid = true;
+  int my_col[2];
+  T my_val[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int p = lane + 32 * h;
+    my_col[h] = -1;
+    my_val[h] = T(0);
+    if (p < size) {
+      const int c = pattern[p];
+      const T t = z[p] / norm;
+      const T val = t * scale[c];
+      my_col[h] = c;
+      my_val[h] = val;
+      if (!isfinite(val)) valid = false;
+      if (p == 0 && !(val > T(0))) valid = false;
+    }
+  }
+  const bool all_valid = __all_sync(0xffffffffu, valid);
+  int32_t* oc = ell_cols + (size_t)i * W;
+  T* ov = ell_vals + (size_t)i * W;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int p = lane + 32 * h;
+    if (p < size) {
+      int rank = 0;
+      for (int q = 0; q < size; ++q) rank += (pattern[q] < my_col[h]);
+      oc[rank] = my_col[h];
+      ov[rank] = my_val[h];
+    } else if (p < W) {
+      oc[p] = -1;
+      ov[p] = T(0);
+    }
+  }
+  if (lane == 0) {
+    row_counts[i] = size;
+    if (truncated) atomicAdd(status + 1, 1);
+    if (!all_valid) atomicAdd(status + 2, 1);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Scans, packing, transpose, scalarise, conversion.
+
+// Exclusive scan of int32 counts into out[0..n] (out[n] = total), 1024 per CTA.
+__global__ void scan_block_kernel(const int32_t* in, int32_t* out, int64_t* block_sums, int n) {
+  __shared__ int64_t buf[1024];
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const int64_t v = (i < n) ? in[i] : 0;
+  buf[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int64_t t = (threadIdx.x >= o) ? buf[threadIdx.x - o] : 0;
+    __syncthreads();
+    buf[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) out[i] = (int32_t)(buf[threadIdx.x] - v);
+  if (threadIdx.x == 1023) block_sums[blockIdx.x] = buf[1023];
+}
+
+__global__ void scan_sums_kernel(int64_t* sums, int nb, int32_t* out_total, int n) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t run = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int64_t t = sums[b];
+    sums[b] = run;
+    run += t;
+  }
+  out_total[n] = (int32_t)run;
+}
+
+__global__ void scan_add_kernel(int32_t* out, const int64_t* sums, int n) {
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] = (int32_t)(out[i] + sums[blockIdx.x]);
+}
+
+}  // namespace
+
+int scan_exclusive_i32(const int32_t* in, int32_t* out, int n, cudaStream_t st) {
+  const int nb = (n + 1023) / 1024;
+  DevBuf sums;
+  int rc = sums.alloc(sizeof(int64_t) * (nb + 1));
+  if (rc) return rc;
+  if (n > 0) scan_block_kernel<<<nb, 1024, 0, st>>>(in, out, sums.as<int64_t>(), n);
+  scan_sums_kernel<<<1, 32, 0, st>>>(sums.as<int64_t>(), nb, out, n);
+  if (n > 0) scan_add_kernel<<<nb, 1024, 0, st>>>(out, sums.as<int64_t>(), n);
+  GBPC_CUDA_TRY(cudaGetLastError());
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));  // `sums` is released on return
+  return GBPC_OK;
+}
+
+namespace {
+
+template <typename T>
+__global__ void pack_kernel(int n, int width, const int32_t* __restrict__ ell_cols,
+                            const T* __restrict__ ell_vals, const int32_t* __restrict__ offsets,
+                            int32_t* columns, T* values) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int b = offsets[i], e_end = offsets[i + 1];
+  for (int e = b; e < e_end; ++e) {
+    const size_t p = (size_t)i * width + (e - b);
+    columns[e] = ell_cols[p];
+    values[e] = ell_vals[p];
+  }
+}
+
+__global__ void count_columns_kernel(int nrow, const int32_t* __restrict__ off,
+                                     const int32_t* __restrict__ col, int32_t* counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrow) return;
+  for (int e = off[i]; e < off[i + 1]; ++e) atomicAdd(counts + col[e], 1);
+}
+
+template <typename T>
+__global__ void scatter_transpose_kernel(int nrow, const int32_t* __restrict__ off,
+                                         const int32_t* __restrict__ col, const T* __restrict__ val,
+                                         int32_t* cursor, int32_t* t_col, T* t_val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrow) return;
+  for (int e = off[i]; e < off[i + 1]; ++e) {
+    const int dst = atomicAdd(cursor + col[e], 1);
+    t_col[dst] = i;
+    t_val[dst] = val[e];
+  }
+}
+
+// Insertion sort of each row by column (rows of a transpose are short).
+template <typename T>
+__global__ void sort_rows_kernel(int nrow, const int32_t* __restrict__ off, int32_t* cols, T* vals) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrow) return;
+  const int b = off[r], e_end = off[r + 1];
+  for (int e = b + 1; e < e_end; ++e) {
+    const int c = cols[e];
+    const T v = vals[e];
+    int q = e;
+    while (q > b && cols[q - 1] > c) {
+      cols[q] = cols[q - 1];
+      vals[q] = vals[q - 1];
+      --q;
+    }
+    cols[q] = c;
+    vals[q] = v;
+  }
+}
+
+// fsai_pack.py:74-107.
+template <typename T>
+__global__ void scalarize_kernel(int nrow_blocks, int b, const int32_t* __restrict__ off,
+                                 const int32_t* __restrict__ col, const T* __restrict__ val,
+                                 int32_t* out_off, int32_t* out_col, T* out_val) {
+  const int n = nrow_blocks * b;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = i / b, component = i % b;
+  const int start = off[r];
+  const int count = off[r + 1] - start;
+  const int64_t base = (int64_t)start * b * b + (int64_t)component * count * b;
+  out_off[i] = (int32_t)base;
+  for (int p = 0; p < count; ++p)
+    for (int c = 0; c < b; ++c) {
+      const int64_t dest = base + (int64_t)p * b + c;
+      out_col[dest] = col[start + p] * b + c;
+      out_val[dest] = val[((int64_t)start + p) * b * b + (int64_t)component * b + c];
+    }
+  if (i == n - 1) out_off[i + 1] = (int32_t)(base + (int64_t)count * b);
+}
+
+template <typename TI, typename TO>
+__device__ __forceinline__ TO narrow(TI v);
+template <> __device__ __forceinline__ float narrow<double, float>(double v) { return __double2float_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 narrow<double, __nv_bfloat16>(double v) {
+  return __float2bfloat16_rn(__double2float_rn(v));
+}
+template <> __device__ __forceinline__ __nv_bfloat16 narrow<float, __nv_bfloat16>(float v) {
+  return __float2bfloat16_rn(v);
+}
+template <> __device__ __forceinline__ double narrow<double, double>(double v) { return v; }
+template <> __device__ __forceinline__ float narrow<float, float>(float v) { return v; }
+
+// fsai.py:181-196: finite values and a positive diagonal after conversion.
+template <typename TI, typename TO>
+__global__ void convert_factor_kernel(int n, const int32_t* __restrict__ off,
+                                      const int32_t* __restrict__ col, const TI* __restrict__ src,
+                                      TO* dst, int32_t* invalid) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  bool bad = false;
+  for (int e = off[row]; e < off[row + 1]; ++e) {
+    const TO v = narrow<TI, TO>(src[e]);
+    dst[e] = v;
+    const float f = to_float(v);
+    if (!isfinite(f)) bad = true;
+    if (col[e] == row && !(f > 0.0f)) bad = true;
+  }
+  if (bad) atomicAdd(invalid, 1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host entry points.
+
+template <typename T>
+static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* val, int W,
+                        int S, double kap, double floor_, int32_t* ell_cols, T* ell_vals,
+                        int32_t* counts, T* scale, int32_t* status_host, cudaStream_t st) {
+  int64_t nnz = 0;
+  {
+    int32_t last = 0;
+    GBPC_CUDA_TRY(cudaMemcpyAsync(&last, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+    nnz = last;
+  }
+  DevBuf ahat, ahatT, status, ovl;
+  int rc;
+  if ((rc = ahat.alloc(sizeof(T) * std::max<int64_t>(nnz, 1)))) return rc;
+  if ((rc = ahatT.alloc(sizeof(T) * std::max<int64_t>(nnz, 1)))) return rc;
+  if ((rc = status.alloc(sizeof(int32_t) * 8))) return rc;
+  if ((rc = ovl.alloc(sizeof(int32_t) * std::max(n, 1)))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int32_t) * 8, st));
+  int32_t* stat = status.as<int32_t>();
+  if (n > 0) {
+    fsai_diag_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, off, col, val, scale, stat);
+    fsai_prep_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, off, col, val, scale, ahat.as<T>(),
+                                                          ahatT.as<T>(), stat);
+  }
+  GBPC_CUDA_TRY(cudaGetLastError());
+  int32_t h[8];
+  GBPC_CUDA_TRY(cudaMemcpyAsync(h, stat, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h[3] != 0) {
+    gbpc_set_error("FSAI setup requires a structurally symmetric matrix (%d entries lack a "
+                   "stored transpose)", h[3]);
+    return GBPC_ERR_UNSUPPORTED;
+  }
+  const int maxrow = std::max(h[4], 1);
+  int PH = 1, pbits = 0;
+  while (PH < 2 * W) { PH <<= 1; ++pbits; }
+  if (pbits == 0) { PH = 2; pbits = 1; }
+  // Distinct candidates never exceed W * maxrow; a table larger than that
+  // cannot overflow.  First pass uses a smaller table for occupancy.
+  int64_t bound = (int64_t)W * maxrow + 1;
+  int Hfull = 32, hbits_full = 5;
+  while (Hfull < bound) { Hfull <<= 1; ++hbits_full; }
+  int Hfirst = Hfull, hbits_first = hbits_full;
+  const int Hcap = (W <= 16) ? 512 : 1024;
+  while (Hfirst > Hcap) { Hfirst >>= 1; --hbits_first; }
+
+  int smem_optin = 0, dev = 0;
+  GBPC_CUDA_TRY(cudaGetDevice(&dev));
+  GBPC_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+
+  auto launch = [&](int H, int hbits, const int32_t* rows, int nrows) -> int {
+    const size_t per_warp = warp_smem_bytes<T>(W, S, H, PH);
+    if (per_warp > (size_t)smem_optin) {
+      gbpc_set_error("FSAI setup: rows too long for shared memory (%zu bytes per warp)", per_warp);
+      return GBPC_ERR_UNSUPPORTED;
+    }
+    int warps = (int)std::min<size_t>(8, std::max<size_t>(1, (100 * 1024) / per_warp));
+    while ((size_t)warps * per_warp > (size_t)smem_optin) --warps;
+    const size_t smem = (size_t)warps * per_warp;
+    GBPC_CUDA_TRY(cudaFuncSetAttribute(fsai_build_kernel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BuildParams P;
+    P.n = n;
+    P.width = W;
+    P.step = S;
+    P.hsize = H;
+    P.hbits = hbits;
+    P.psize = PH;
+    P.pbits = pbits;
+    P.rows = rows;
+    P.nrows_list = nrows;
+    P.overflow_list = ovl.as<int32_t>();
+    P.overflow_count = stat + 5;
+    const int items = rows ? nrows : n;
+    if (items > 0)
+      fsai_build_kernel<T><<<grid_for(items, warps), warps * 32, smem, st>>>(
+          P, off, col, ahat.as<T>(), ahatT.as<T>(), scale, (T)kap, (T)floor_, ell_cols, ell_vals,
+          counts, stat);
+    GBPC_CUDA_TRY(cudaGetLastError());
+    return GBPC_OK;
+  };
+  if ((rc = launch(Hfirst, hbits_first, nullptr, n))) return rc;
+  GBPC_CUDA_TRY(cudaMemcpyAsync(h, stat, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h[5] > 0) {
+    // Rows whose frontier overflowed the first table: rerun them exactly
+    // with a table that cannot overflow.
+    const int nover = h[5];
+    DevBuf list;
+    if ((rc = list.alloc(sizeof(int32_t) * nover))) return rc;
+    GBPC_CUDA_TRY(cudaMemcpyAsync(list.p, ovl.p, sizeof(int32_t) * nover, cudaMemcpyDeviceToDevice, st));
+    GBPC_CUDA_TRY(cudaMemsetAsync(stat + 5, 0, sizeof(int32_t), st));
+    if ((rc = launch(Hfull, hbits_full, list.as<int32_t>(), nover))) return rc;
+    GBPC_CUDA_TRY(cudaMemcpyAsync(h, stat, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h[5] > 0) {
+      gbpc_set_error("FSAI setup: candidate table overflow");
+      return GBPC_ERR_UNSUPPORTED;
+    }
+  }
+  if (status_host) {
+    status_host[0] = h[0];
+    status_host[1] = h[1];
+    status_host[2] = h[2];
+  }
+  if (h[0]) {
+    gbpc_set_error("FSAI requires finite positive diagonals (%d invalid rows)", h[0]);
+    return GBPC_ERR_DIAGONAL;
+  }
+  if (h[2]) {
+    gbpc_set_error("FSAI factor lost finite entries or a positive diagonal");
+    return GBPC_ERR_FACTOR;
+  }
+  return GBPC_OK;
+}
+
+}  // namespace gbpc
+
+using namespace gbpc;
+
+extern "C" int gbpc_fsai_setup(int n, const int32_t* offsets, const int32_t* columns,
+                               const void* values, int dtype, int width, int step,
+                               double kap_tolerance, double pivot_floor, int32_t* ell_cols,
+                               void* ell_vals, int32_t* row_counts, void* scale,
+                               int32_t* status_host, void* stream) {
+  if (n < 0 || !offsets || (n > 0 && (!columns || !values || !ell_cols || !ell_vals ||
+                                      !row_counts || !scale))) {
+    gbpc_set_error("gbpc_fsai_setup: null or negative argument");
+    return GBPC_ERR_ARG;
+  }
+  if (width < 1 || width > 64) {
+    gbpc_set_error("max_row_size must be an integer in [1, 64]");
+    return GBPC_ERR_ARG;
+  }
+  if (step < 1 || step > 64) {
+    gbpc_set_error("max_step_size must be an integer in [1, 64]");
+    return GBPC_ERR_ARG;
+  }
+  if (!(kap_tolerance >= 0.0 && kap_tolerance < 1.0)) {
+    gbpc_set_error("kap_tolerance must be in [0, 1)");
+    return GBPC_ERR_ARG;
+  }
+  if (!(pivot_floor > 0.0 && pivot_floor < 1.0)) {
+    gbpc_set_error("pivot_floor must be in (0, 1)");
+    return GBPC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GBPC_F64)
+    return fsai_setup_t<double>(n, offsets, columns, (const double*)values, width, step,
+                                kap_tolerance, pivot_floor, ell_cols, (double*)ell_vals,
+                                row_counts, (double*)scale, status_host, st);
+  if (dtype == GBPC_F32)
+    return fsai_setup_t<float>(n, offsets, columns, (const float*)values, width, step,
+                               kap_tolerance, pivot_floor, ell_cols, (float*)ell_vals,
+                               row_counts, (float*)scale, status_host, st);
+  gbpc_set_error("FSAI supports float32 and float64 matrices");
+  return GBPC_ERR_ARG;
+}
+
+extern "C" int gbpc_fsai_pack(int n, int width, const int32_t* ell_cols, const void* ell_vals,
+                              const int32_t* row_counts, int dtype, int32_t* offsets_out,
+                              int32_t* columns_out, void* values_out, int64_t* nnz_host,
+                              void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n < 0 || !offsets_out || (n > 0 && !row_counts)) {
+    gbpc_set_error("gbpc_fsai_pack: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  if (columns_out == nullptr) {
+    int rc = scan_exclusive_i32(row_counts, offsets_out, n, st);
+    if (rc) return rc;
+    int32_t total = 0;
+    GBPC_CUDA_TRY(cudaMemcpyAsync(&total, offsets_out + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (nnz_host) *nnz_host = total;
+    return GBPC_OK;
+  }
+  if (n == 0) return GBPC_OK;
+  if (dtype == GBPC_F64)
+    pack_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(n, width, ell_cols, (const double*)ell_vals,
+                                                         offsets_out, columns_out, (double*)values_out);
+  else if (dtype == GBPC_F32)
+    pack_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, width, ell_cols, (const float*)ell_vals,
+                                                        offsets_out, columns_out, (float*)values_out);
+  else {
+    gbpc_set_error("gbpc_fsai_pack: dtype must be float64 or float32");
+    return GBPC_ERR_ARG;
+  }
+  GBPC_CUDA_TRY(cudaGetLastError());
+  return GBPC_OK;
+}
+
+template <typename T>
+static int transpose_t(int nrow, int ncol, const int32_t* off, const int32_t* col, const T* val,
+                       int32_t* t_off, int32_t* t_col, T* t_val, cudaStream_t st) {
+  DevBuf counts, cursor;
+  int rc;
+  if ((rc = counts.alloc(sizeof(int32_t) * (ncol + 1)))) return rc;
+  if ((rc = cursor.alloc(sizeof(int32_t) * (ncol + 1)))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(counts.p, 0, sizeof(int32_t) * (ncol + 1), st));
+  if (nrow > 0) count_columns_kernel<<<grid_for(nrow, 256), 256, 0, st>>>(nrow, off, col, counts.as<int32_t>());
+  GBPC_CUDA_TRY(cudaGetLastError());
+  if ((rc = scan_exclusive_i32(counts.as<int32_t>(), t_off, ncol, st))) return rc;
+  GBPC_CUDA_TRY(cudaMemcpyAsync(cursor.p, t_off, sizeof(int32_t) * (ncol + 1), cudaMemcpyDeviceToDevice, st));
+  if (nrow > 0)
+    scatter_transpose_kernel<T><<<grid_for(nrow, 256), 256, 0, st>>>(nrow, off, col, val,
+                                                                    cursor.as<int32_t>(), t_col, t_val);
+  if (ncol > 0) sort_rows_kernel<T><<<grid_for(ncol, 256), 256, 0, st>>>(ncol, t_off, t_col, t_val);
+  GBPC_CUDA_TRY(cudaGetLastError());
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_csr_transpose(int nrow, int ncol, const int32_t* offsets,
+                                  const int32_t* columns, const void* values, int dtype,
+                                  int32_t* t_off, int32_t* t_col, void* t_val, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nrow < 0 || ncol < 0 || !offsets || !t_off) {
+    gbpc_set_error("gbpc_csr_transpose: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  switch (dtype) {
+    case GBPC_F64:
+      return transpose_t<double>(nrow, ncol, offsets, columns, (const double*)values, t_off, t_col,
+                                 (double*)t_val, st);
+    case GBPC_F32:
+      return transpose_t<float>(nrow, ncol, offsets, columns, (const float*)values, t_off, t_col,
+                                (float*)t_val, st);
+    case GBPC_BF16:
+      return transpose_t<__nv_bfloat16>(nrow, ncol, offsets, columns, (const __nv_bfloat16*)values,
+                                        t_off, t_col, (__nv_bfloat16*)t_val, st);
+  }
+  gbpc_set_error("gbpc_csr_transpose: bad dtype");
+  return GBPC_ERR_ARG;
+}
+
+extern "C" int gbpc_scalarize(int nrow_blocks, int b, const int32_t* offsets,
+                              const int32_t* columns, const void* values, int dtype,
+                              int32_t* out_off, int32_t* out_col, void* out_val, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nrow_blocks < 0 || b < 1 || b > 8 || !offsets || !out_off) {
+    gbpc_set_error("gbpc_scalarize: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  const int n = nrow_blocks * b;
+  if (n == 0) {
+    GBPC_CUDA_TRY(cudaMemsetAsync(out_off, 0, sizeof(int32_t), st));
+    return GBPC_OK;
+  }
+  if (dtype == GBPC_F64)
+    scalarize_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(nrow_blocks, b, offsets, columns,
+                                                              (const double*)values, out_off,
+                                                              out_col, (double*)out_val);
+  else if (dtype == GBPC_F32)
+    scalarize_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(nrow_blocks, b, offsets, columns,
+                                                             (const float*)values, out_off, out_col,
+                                                             (float*)out_val);
+  else {
+    gbpc_set_error("gbpc_scalarize: dtype must be float64 or float32");
+    return GBPC_ERR_ARG;
+  }
+  GBPC_CUDA_TRY(cudaGetLastError());
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_convert_factor(int n, const int32_t* offsets, const int32_t* columns,
+                                   const void* src, int src_dtype, void* dst, int dst_dtype,
+                                   int32_t* invalid_host, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf bad;
+  int rc;
+  if ((rc = bad.alloc(sizeof(int32_t)))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(bad.p, 0, sizeof(int32_t), st));
+  if (n > 0) {
+    const int g = grid_for(n, 256);
+    if (src_dtype == GBPC_F64 && dst_dtype == GBPC_F32)
+      convert_factor_kernel<double, float><<<g, 256, 0, st>>>(n, offsets, columns, (const double*)src,
+                                                             (float*)dst, bad.as<int32_t>());
+    else if (src_dtype == GBPC_F64 && dst_dtype == GBPC_BF16)
+      convert_factor_kernel<double, __nv_bfloat16><<<g, 256, 0, st>>>(
+          n, offsets, columns, (const double*)src, (__nv_bfloat16*)dst, bad.as<int32_t>());
+    else if (src_dtype == GBPC_F32 && dst_dtype == GBPC_BF16)
+      convert_factor_kernel<float, __nv_bfloat16><<<g, 256, 0, st>>>(
+          n, offsets, columns, (const float*)src, (__nv_bfloat16*)dst, bad.as<int32_t>());
+    else if (src_dtype == dst_dtype && src_dtype == GBPC_F64)
+      convert_factor_kernel<double, double><<<g, 256, 0, st>>>(n, offsets, columns, (const double*)src,
+                                                              (double*)dst, bad.as<int32_t>());
+    else if (src_dtype == dst_dtype && src_dtype == GBPC_F32)
+      convert_factor_kernel<float, float><<<g, 256, 0, st>>>(n, offsets, columns, (const float*)src,
+                                                            (float*)dst, bad.as<int32_t>());
+    else {
+      gbpc_set_error("gbpc_convert_factor: unsupported conversion %d -> %d", src_dtype, dst_dtype);
+      return GBPC_ERR_ARG;
+    }
+  }
+  GBPC_CUDA_TRY(cudaGetLastError());
+  int32_t h = 0;
+  GBPC_CUDA_TRY(cudaMemcpyAsync(&h, bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  if (invalid_host) *invalid_host = h;
+  if (h) {
+    gbpc_set_error("factor_dtype conversion lost finite entries or a positive diagonal");
+    return GBPC_ERR_CONVERSION;
+  }
+  return GBPC_OK;
+}

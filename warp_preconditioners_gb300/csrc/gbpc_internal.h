@@ -1,0 +1,125 @@
+// Host-side internals shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <vector>
+
+#include "../../include/gbpc.h"
+
+namespace gbpc {
+
+constexpr int kMaxCtas = 152 * 8;  // partial-sum capacity of every reduction buffer
+
+size_t dtype_size(int dtype);
+bool valid_value_dtype(int d);
+
+// Owned device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int alloc(size_t n);
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Sliced ELL matrix (32 block rows per slice) with owned storage.
+struct Sell {
+  int nrow = 0;     // block rows
+  int ncol = 0;     // block columns
+  int B = 1;        // block size
+  int nslices = 0;
+  int vdtype = GBPC_F64;
+  int64_t nent = 0;  // entries including padding
+  DevBuf slice_ptr;  // int64[nslices + 1]
+  DevBuf cols;       // int32[nent]
+  DevBuf vals;       // vdtype[nent * B * B]
+};
+
+// Build options: output row k reads source row rows[k] (rows == nullptr:
+// k itself); columns are remapped through colmap (entries whose image is
+// negative are dropped); `part` keeps all (0), strictly lower (1) or strictly
+// upper (2) blocks relative to the source row index.
+struct SellBuild {
+  const int32_t* rows = nullptr;
+  const int32_t* colmap = nullptr;
+  int part = 0;
+};
+
+int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,
+               const void* val, int in_dtype, int out_dtype, const SellBuild& opt,
+               cudaStream_t st);
+
+// Epilogues of the SELL product (see gbpc_sell.cu).
+enum EpiKind : int {
+  EPI_AXPBY = 0,      // z = alpha * acc + beta * y
+  EPI_SQLAP_FWD = 1,  // z = aux0 * acc                      (aux0 = 1/mass)
+  EPI_SQLAP_BWD = 2,  // z = alpha * (acc + aux0 * aux1) + beta * y  (aux0 = w*mass[free], aux1 = x)
+  EPI_TRI_LOWER = 3,  // z = aux0 - acc                      (aux0 = rhs)
+  EPI_TRI_UPPER = 4,  // z = inv_block(aux1) * (aux0 - acc)  (aux0 = rhs, aux1 = inverse blocks)
+};
+
+struct EpiHost {
+  int kind = EPI_AXPBY;
+  const void* aux0 = nullptr;
+  const void* aux1 = nullptr;
+};
+
+struct ReductionHost;  // defined in gbpc_common.cuh as gbpc::Reduction
+
+// Scratch for one deterministic reduction: partials + arrival counter.
+struct ReduceBuf {
+  DevBuf partials;  // double[kMaxCtas]
+  DevBuf counter;   // unsigned int[1], zero between uses
+  int init(cudaStream_t st);
+};
+
+// z = alpha * A x + beta * y over a SELL matrix with vector type adtype.
+// red_w != nullptr adds dot(red_w, z) reduced into `rb` with finalize mode
+// `fin_mode` acting on `ks` (or storing to `fin_out`).
+struct DotSpec {
+  const double* w = nullptr;
+  ReduceBuf* rb = nullptr;
+  int mode = 0;
+  void* ks = nullptr;
+  double* out = nullptr;
+};
+
+int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, double alpha,
+              double beta, const int* guard, const EpiHost& ep, const DotSpec* dot,
+              cudaStream_t st);
+
+// Vector helpers (float64 unless stated).
+int vec_copy(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Operators.
+
+struct Operator {
+  virtual ~Operator() = default;
+  int64_t rows = 0;        // scalar vector length
+  int vdtype = GBPC_F64;   // vector dtype
+  // z = alpha Op x + beta y.  `guard` (nullable device int) skips all work
+  // when zero.  `dot` (nullable) reduces dot(dot->w, z) in the final kernel.
+  virtual int apply(const void* x, const void* y, void* z, double alpha, double beta,
+                    const int* guard, const DotSpec* dot, cudaStream_t st) = 0;
+  // True when x may not alias z in apply (the generic entry copies x first).
+  virtual bool gathers_x() const { return true; }
+  DevBuf alias_scratch;  // copy of x when x aliases z
+};
+
+}  // namespace gbpc
+
+struct gbpc_op {
+  std::unique_ptr<gbpc::Operator> impl;
+};

@@ -1,0 +1,154 @@
+"""LinearOperator protocol and the CG / CR entry points.
+
+Mirrors the parts of ``warp.optim.linear`` that the reference uses: the
+``LinearOperator(shape, dtype, device, matvec)`` base with
+``matvec(x, y, z, alpha, beta)`` computing ``z = alpha * Op x + beta * y``,
+``aslinearoperator``, ``preconditioner(A, "diag")`` and ``cg`` / ``cr`` with
+the same signature and return values (device arrays when ``check_every=0``).
+The loops themselves run in libgbpc (one CUDA graph per solve).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import torch
+
+from . import _lib
+from .sparse import BsrMatrix
+
+
+class LinearOperator:
+    def __init__(self, shape, dtype, device, matvec):
+        self.shape = tuple(shape)
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self._matvec = matvec
+
+    @property
+    def scalar_type(self) -> torch.dtype:
+        return self.dtype
+
+    def matvec(self, x, y, z, alpha, beta):
+        self._matvec(x, y, z, alpha, beta)
+
+    # Subclasses backed by libgbpc set `_op` (an _lib.OpHandle).
+    _op = None
+
+
+class _HandleOperator(LinearOperator):
+    """A LinearOperator whose apply is one libgbpc operator."""
+
+    def __init__(self, handle: _lib.OpHandle, shape, dtype, device):
+        self._op = handle
+        super().__init__(shape, dtype, device, self._apply)
+
+    def _apply(self, x, y, z, alpha, beta):
+        self._op.apply(_flat(x), _flat(y) if y is not None else None, _flat(z), alpha, beta,
+                       self.device)
+
+
+def _flat(t: torch.Tensor) -> torch.Tensor:
+    if not t.is_contiguous():
+        raise ValueError("vectors must be contiguous")
+    return t.view(-1)
+
+
+def aslinearoperator(a) -> LinearOperator | None:
+    """BsrMatrix -> sparse-product operator; LinearOperators pass through."""
+    if a is None or isinstance(a, LinearOperator):
+        return a
+    if isinstance(a, BsrMatrix):
+        cached = getattr(a, "_gbpc_linop", None)
+        if cached is not None:
+            return cached
+        b = a.block_shape[0]
+        dt = a.scalar_type
+        h = _lib.new_op("gbpc_op_sparse", a.nrow, a.ncol, b, _lib.ptr(a.offsets),
+                        _lib.ptr(a.columns), _lib.ptr(a.values), _lib.dtype_code(dt),
+                        _lib.dtype_code(dt), _lib.stream(a.device))
+        op = _HandleOperator(h, a.shape, dt, a.device)
+        a._gbpc_linop = op
+        return op
+    raise TypeError(f"cannot make a linear operator from {type(a).__name__}")
+
+
+def preconditioner(A, ptype="diag") -> LinearOperator:
+    """Scalar Jacobi preconditioner on the scalar diagonal of A."""
+    if ptype != "diag":
+        raise ValueError(f"unsupported preconditioner type {ptype!r}")
+    if not isinstance(A, BsrMatrix):
+        raise TypeError("preconditioner() needs a BsrMatrix")
+    b = A.block_shape[0]
+    h = _lib.new_op("gbpc_op_diagonal", A.nrow, b, _lib.ptr(A.offsets), _lib.ptr(A.columns),
+                    _lib.ptr(A.values), _lib.dtype_code(A.scalar_type), _lib.stream(A.device))
+    return _HandleOperator(h, A.shape, A.scalar_type, A.device)
+
+
+def _handle(op: LinearOperator | None):
+    if op is None:
+        return None
+    h = getattr(op, "_op", None)
+    if h is None:
+        raise TypeError(f"{type(op).__name__} has no libgbpc operator")
+    return h.handle
+
+
+class Solver:
+    """Reusable CG / CR solver bound to (A, M); repeated runs replay one graph."""
+
+    def __init__(self, method: str, A, M=None, use_cuda_graph=True):
+        self.A = aslinearoperator(A)
+        self.M = aslinearoperator(M)
+        code = _lib.GBPC_CG if method == "cg" else _lib.GBPC_CR
+        out = ctypes.c_void_p()
+        _lib.call("gbpc_solver_create", code, _handle(self.A), _handle(self.M),
+                  int(bool(use_cuda_graph)), _lib.stream(self.A.device), ctypes.byref(out))
+        self._h = out
+        dev = self.A.device
+        self.nit = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.rr = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.atol_sq = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbpc_solver_destroy(h)
+            except Exception:
+                pass
+
+    def run(self, b, x, tol=None, atol=None, maxiter=0):
+        tol = 1.0e-5 if tol is None else float(tol)
+        atol = 0.0 if atol is None else float(atol)
+        _lib.call("gbpc_solver_run", self._h, _lib.ptr(_flat(b)), _lib.ptr(_flat(x)), tol, atol,
+                  int(maxiter), _lib.ptr(self.nit), _lib.ptr(self.rr), _lib.ptr(self.atol_sq),
+                  _lib.stream(self.A.device))
+        return self.nit, self.rr, self.atol_sq
+
+
+def _solve(method, A, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph):
+    if callback is not None:
+        raise NotImplementedError("per-iteration callbacks are not supported; the loop runs on "
+                                  "the device")
+    if b.dtype != torch.float64 or x.dtype != torch.float64:
+        raise TypeError("cg/cr run on float64 vectors")
+    s = Solver(method, A, M, use_cuda_graph)
+    nit, rr, atol_sq = s.run(b, x, tol, atol, maxiter)
+    if check_every == 0:
+        return nit.clone(), rr.clone(), atol_sq.clone()
+    vals = torch.stack([nit.to(torch.float64), rr, atol_sq]).cpu()
+    return int(vals[0]), math.sqrt(max(float(vals[1]), 0.0)), math.sqrt(float(vals[2]))
+
+
+def cg(A, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+       use_cuda_graph=True):
+    """Preconditioned conjugate gradient (warp.optim.linear.cg signature)."""
+    return _solve("cg", A, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+
+
+def cr(A, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+       use_cuda_graph=True):
+    """Preconditioned conjugate residual (warp.optim.linear.cr signature)."""
+    return _solve("cr", A, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
