@@ -110,9 +110,22 @@ def test_biharmonic_tet_cube_solve(oracle):
     pre = FSAI(to_bsr(q), max_row_size=8)
     rhs = problems.smoothing_rhs(verts, mass, alpha)
     solver = linear.Solver("cg", op, pre)
+    qc = oracle_csr(oracle, q)
+    g, gt, _ = oracle.fsai(qc, width=8)
+    kc = oracle_csr(oracle, K)
     for k in range(4):
         x = torch.zeros(n, dtype=torch.float64, device=cuda())
         nit, rr, atol_sq = solver.run(vec(rhs[k]), x, tol=1e-8, maxiter=20000)
         assert rr.item() <= atol_sq.item()
         sol = x.cpu().numpy()
-        assert np.linalg.norm(rhs[k] - q @ sol) <= 1e-7 * np.linalg.norm(rhs[k])
+        # This operator is so ill-conditioned that b - Q x evaluated in float64
+        # is dominated by cancellation (the reference reports the same gap
+        # between recursive and recomputed residuals); the componentwise
+        # backward error (benchmarks/dragon.py:34-37) is the accuracy measure.
+        berr = np.max(np.abs(rhs[k] - q @ sol) / (abs(q) @ np.abs(sol) + np.abs(rhs[k])))
+        assert berr < 1e-13
+        x_or, it_or, _, _ = oracle.krylov("cg", oracle.Operator.sqlap(kc, mass, alpha), rhs[k],
+                                          M=oracle.Operator.fsai(g, gt), tol=1e-8, maxiter=20000)
+        berr_or = np.max(np.abs(rhs[k] - q @ x_or) / (abs(q) @ np.abs(x_or) + np.abs(rhs[k])))
+        assert berr < 10 * berr_or + 1e-15
+        assert abs(int(nit.item()) - it_or) <= max(3, it_or // 50)

@@ -252,7 +252,9 @@ def test_block_ilu0_bsr_matches_oracle(oracle):
     pre.matvec(vec(x), vec(x), z, 1.0, 0.0)
     ref = oracle.bilu0_apply(nrow, 3, bsr.indptr, bsr.indices, f_or, inv_or, 3, x,
                              np.zeros_like(x), 1.0, 0.0)
-    np.testing.assert_allclose(z.cpu().numpy(), ref, rtol=1e-10, atol=1e-12)
+    # C = R diag(1, 1, 1e-6) R^T: the inverse blocks amplify summation-order
+    # differences by about 1e6, so agreement is to ~1e-16 * 1e6 * sweeps.
+    np.testing.assert_allclose(z.cpu().numpy(), ref, rtol=1e-7, atol=1e-9)
 
 
 @pytest.mark.parametrize("blocks", [1, 2, 4])
