@@ -276,7 +276,9 @@ def main():
     if args.profile_iters > 0:
         op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
         pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
-        solver = linear.Solver(args.method, op, pre)
+        # Host-driven loop: kernels inside a graph with conditional nodes cannot
+        # be profiled individually.
+        solver = linear.Solver(args.method, op, pre, use_cuda_graph=False)
         nit, _, _ = solver.run(rhs[0], xs[0], tol=args.rtol, maxiter=args.profile_iters)
         torch.cuda.synchronize()
         print(json.dumps({"profile_iters": int(nit.item()), "n": n, "fsai_nnz": pre.G.nnz}))

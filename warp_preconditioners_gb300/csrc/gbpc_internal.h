@@ -49,11 +49,13 @@ struct Sell {
 // Build options: output row k reads source row rows[k] (rows == nullptr:
 // k itself); columns are remapped through colmap (entries whose image is
 // negative are dropped); `part` keeps all (0), strictly lower (1) or strictly
-// upper (2) blocks relative to the source row index.
+// upper (2) blocks relative to the source row index; `row_scale` multiplies
+// every value of source row r by row_scale[r] (bf16 input: unsupported).
 struct SellBuild {
   const int32_t* rows = nullptr;
   const int32_t* colmap = nullptr;
   int part = 0;
+  const void* row_scale = nullptr;  // optional per-source-row factor (input value dtype)
 };
 
 int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,

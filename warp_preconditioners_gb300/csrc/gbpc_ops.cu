@@ -209,8 +209,8 @@ struct SqlapOp : Operator {
             const DotSpec* dot, cudaStream_t st) override {
     int rc;
     if (alpha != 0.0) {
-      EpiHost f{EPI_SQLAP_FWD, inv_mass.p, nullptr};
-      rc = sell_spmv(fwd, vdtype, x, nullptr, tmp.p, 1.0, 0.0, guard, f, nullptr, st);
+      // tmp = (M^-1 L) x with the row scaling folded into the stored values.
+      rc = sell_spmv(fwd, vdtype, x, nullptr, tmp.p, 1.0, 0.0, guard, EpiHost{}, nullptr, st);
       if (rc) return rc;
     }
     EpiHost b{EPI_SQLAP_BWD, wmass.p, x};
@@ -218,8 +218,7 @@ struct SqlapOp : Operator {
   }
   bool gathers_x() const override { return false; }
   int rhs(const void* u, void* out, cudaStream_t st) {
-    EpiHost f{EPI_SQLAP_FWD, inv_mass.p, nullptr};
-    int rc = sell_spmv(bnd, vdtype, u, nullptr, tmp.p, 1.0, 0.0, nullptr, f, nullptr, st);
+    int rc = sell_spmv(bnd, vdtype, u, nullptr, tmp.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);
     if (rc) return rc;
     EpiHost b{EPI_SQLAP_BWD, zeros.p, zeros.p};
     return sell_spmv(bwd, vdtype, tmp.p, nullptr, out, -1.0, 0.0, nullptr, b, nullptr, st);
@@ -479,10 +478,12 @@ extern "C" int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* colum
     boundary_map_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, op->index.as<int32_t>(), bmap.as<int32_t>());
   SellBuild fo;
   fo.colmap = op->index.as<int32_t>();
+  fo.row_scale = op->inv_mass.p;
   SellBuild bo;
   bo.rows = op->free_idx.as<int32_t>();
   SellBuild bd;
   bd.colmap = bmap.as<int32_t>();
+  bd.row_scale = op->inv_mass.p;
   if ((rc = sell_build(op->fwd, n, nfree, 1, offsets, columns, values, dtype, dtype, fo, st))) return fail(rc);
   if ((rc = sell_build(op->bwd, nfree, n, 1, offsets, columns, values, dtype, dtype, bo, st))) return fail(rc);
   if ((rc = sell_build(op->bnd, n, n, 1, offsets, columns, values, dtype, dtype, bd, st))) return fail(rc);

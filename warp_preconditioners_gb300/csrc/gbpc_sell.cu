@@ -156,8 +156,8 @@ template <typename VI, typename VO>
 __global__ void sell_fill_kernel(int nrow, int nslices, int B, const int32_t* __restrict__ off,
                                  const int32_t* __restrict__ col, const VI* __restrict__ val,
                                  const int32_t* rows, const int32_t* colmap, int part,
-                                 const int64_t* __restrict__ slice_ptr, int32_t* cols_out,
-                                 VO* vals_out) {
+                                 const VI* row_scale, const int64_t* __restrict__ slice_ptr,
+                                 int32_t* cols_out, VO* vals_out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int s = r / kSlice;
   if (s >= nslices) return;
@@ -177,9 +177,11 @@ __global__ void sell_fill_kernel(int nrow, int nslices, int B, const int32_t* __
       }
       const int64_t E = base + (int64_t)k * kSlice + lane;
       cols_out[E] = c;
-      for (int q = 0; q < BB; ++q)
-        vals_out[base * BB + ((int64_t)k * BB + q) * kSlice + lane] =
-            convert_value<VI, VO>(val[(int64_t)e * BB + q]);
+      for (int q = 0; q < BB; ++q) {
+        VI v = val[(int64_t)e * BB + q];
+        if (row_scale) v = v * row_scale[src];
+        vals_out[base * BB + ((int64_t)k * BB + q) * kSlice + lane] = convert_value<VI, VO>(v);
+      }
       ++k;
     }
   }
@@ -197,7 +199,7 @@ static void launch_fill(const Sell& s, int B, const int32_t* off, const int32_t*
   const int threads = s.nslices * kSlice;
   sell_fill_kernel<VI, VO><<<grid_for(threads, kThreads), kThreads, 0, st>>>(
       s.nrow, s.nslices, B, off, col, (const VI*)val, opt.rows, opt.colmap, opt.part,
-      s.slice_ptr.as<int64_t>(), s.cols.as<int32_t>(), s.vals.as<VO>());
+      (const VI*)opt.row_scale, s.slice_ptr.as<int64_t>(), s.cols.as<int32_t>(), s.vals.as<VO>());
 }
 
 int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,
@@ -251,6 +253,13 @@ int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const
 
 // ---------------------------------------------------------------------------
 // The sliced product.
+//
+// One warp per slice, slices distributed over a grid that fills the GPU.  For
+// each chunk of entries the warp first issues every column-index load, then
+// every value load and x gather, then the FMAs, so each lane keeps a whole
+// chunk of independent memory requests in flight.  alpha/beta tests are
+// uniform integer flags computed on the host: FP64 compares would take FP64
+// issue slots, the scarce resource on this GPU.
 
 template <typename A>
 struct EpiDev {
@@ -263,14 +272,23 @@ __device__ __forceinline__ A fma_t(A a, A b, A c);
 template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
-// Rows per warp before moving to the next slice group: every warp walks
-// slices warp_id, warp_id + total_warps, ...
-template <int B, typename V, typename A, int EPI>
+enum SpmvFlags : int { F_ALPHA_ZERO = 1, F_ALPHA_ONE = 2, F_BETA_ZERO = 4 };
+
+template <int B> struct Chunk { static constexpr int value = 8; };
+template <> struct Chunk<2> { static constexpr int value = 4; };
+template <> struct Chunk<3> { static constexpr int value = 2; };
+template <> struct Chunk<4> { static constexpr int value = 2; };
+
+template <int B, typename V, typename A, int EPI, bool DOT>
 __global__ void __launch_bounds__(kThreads)
-sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, const int* guard,
-                 EpiDev<A> ep, Reduction red) {
+sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
+                 const int* guard, EpiDev<A> ep, Reduction red) {
   if (guard_off(guard)) return;
   constexpr int BB = B * B;
+  constexpr int CH = Chunk<B>::value;
+  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   double dot_part = 0.0;
@@ -278,48 +296,36 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, c
     const int row = s * kSlice + lane;
     const int64_t base = __ldg(m.slice_ptr + s);
     const int width = (int)((__ldg(m.slice_ptr + s + 1) - base) >> 5);
-    A acc0[B], acc1[B];
+    A acc[B];
 #pragma unroll
-    for (int r = 0; r < B; ++r) {
-      acc0[r] = A(0);
-      acc1[r] = A(0);
-    }
-    const bool run = (EPI == EPI_SQLAP_FWD || EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER)
-                         ? true
-                         : (alpha != A(0));
-    if (run && row < m.nrow) {
+    for (int r = 0; r < B; ++r) acc[r] = A(0);
+    if (run) {
       const int32_t* cp = m.cols + base + lane;
       const V* vp = m.vals + base * BB + lane;
-      int k = 0;
-      for (; k + 1 < width; k += 2) {
-        const int c0 = __ldg(cp + (int64_t)k * kSlice);
-        const int c1 = __ldg(cp + (int64_t)(k + 1) * kSlice);
-        if (c0 >= 0) {
+      for (int k0 = 0; k0 < width; k0 += CH) {
+        int c[CH];
 #pragma unroll
-          for (int r = 0; r < B; ++r)
+        for (int j = 0; j < CH; ++j)
+          c[j] = (k0 + j < width) ? __ldg(cp + (int64_t)(k0 + j) * kSlice) : -1;
+        A xv[CH][B];
+        V vv[CH][BB];
 #pragma unroll
-            for (int q = 0; q < B; ++q)
-              acc0[r] = fma_t<A>(widen<A, V>(__ldg(vp + ((int64_t)k * BB + r * B + q) * kSlice)),
-                                 __ldg(x + (int64_t)c0 * B + q), acc0[r]);
+        for (int j = 0; j < CH; ++j) {
+#pragma unroll
+          for (int q = 0; q < B; ++q) xv[j][q] = (c[j] >= 0) ? __ldg(x + (int64_t)c[j] * B + q) : A(0);
+#pragma unroll
+          for (int q = 0; q < BB; ++q)
+            vv[j][q] = (k0 + j < width) ? __ldg(vp + ((int64_t)(k0 + j) * BB + q) * kSlice)
+                                        : static_cast<V>(0.0f);
         }
-        if (c1 >= 0) {
 #pragma unroll
-          for (int r = 0; r < B; ++r)
+        for (int j = 0; j < CH; ++j) {
+          if (k0 + j < width) {  // uniform across the warp
 #pragma unroll
-            for (int q = 0; q < B; ++q)
-              acc1[r] = fma_t<A>(widen<A, V>(__ldg(vp + ((int64_t)(k + 1) * BB + r * B + q) * kSlice)),
-                                 __ldg(x + (int64_t)c1 * B + q), acc1[r]);
-        }
-      }
-      if (k < width) {
-        const int c0 = __ldg(cp + (int64_t)k * kSlice);
-        if (c0 >= 0) {
+            for (int r = 0; r < B; ++r)
 #pragma unroll
-          for (int r = 0; r < B; ++r)
-#pragma unroll
-            for (int q = 0; q < B; ++q)
-              acc0[r] = fma_t<A>(widen<A, V>(__ldg(vp + ((int64_t)k * BB + r * B + q) * kSlice)),
-                                 __ldg(x + (int64_t)c0 * B + q), acc0[r]);
+              for (int q = 0; q < B; ++q) acc[r] = fma_t<A>(widen<A, V>(vv[j][r * B + q]), xv[j][q], acc[r]);
+          }
         }
       }
     }
@@ -327,23 +333,23 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, c
       A out[B];
 #pragma unroll
       for (int r = 0; r < B; ++r) {
-        const A acc = acc0[r] + acc1[r];
         const int64_t idx = (int64_t)row * B + r;
         if (EPI == EPI_AXPBY) {
-          A v = alpha * acc;
-          if (beta != A(0)) v = fma_t<A>(beta, y[idx], v);
+          A v = alpha_one ? acc[r] : alpha * acc[r];
+          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
           out[r] = v;
-        } else if (EPI == EPI_SQLAP_FWD) {
-          out[r] = ep.aux0[idx] * acc;
         } else if (EPI == EPI_SQLAP_BWD) {
           A v = A(0);
-          if (alpha != A(0)) v = alpha * fma_t<A>(ep.aux0[idx], ep.aux1[idx], acc);
-          if (beta != A(0)) v = fma_t<A>(beta, y[idx], v);
+          if (run) {
+            v = fma_t<A>(ep.aux0[idx], ep.aux1[idx], acc[r]);
+            if (!alpha_one) v = alpha * v;
+          }
+          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
           out[r] = v;
-        } else if (EPI == EPI_TRI_LOWER) {
-          out[r] = ep.aux0[idx] - acc;
+        } else if (EPI == EPI_SQLAP_FWD) {
+          out[r] = ep.aux0[idx] * acc[r];
         } else {
-          out[r] = ep.aux0[idx] - acc;
+          out[r] = ep.aux0[idx] - acc[r];
         }
       }
       if (EPI == EPI_TRI_UPPER) {
@@ -362,20 +368,28 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, c
       for (int r = 0; r < B; ++r) {
         const int64_t idx = (int64_t)row * B + r;
         z[idx] = out[r];
-        if (red.w != nullptr) dot_part = fma((double)out[r], red.w[idx], dot_part);
+        if (DOT) dot_part = fma((double)out[r], red.w[idx], dot_part);
       }
     }
   }
-  if (red.w != nullptr) reduce_and_finalize(red, dot_part);
+  if (DOT) reduce_and_finalize(red, dot_part);
 }
 
 static int spmv_grid(int nslices) {
-  // Two slices per warp when there is enough work; at most kMaxCtas CTAs.
+  // One slice per warp, at most one wave of resident CTAs.
   const int warps_per_cta = kThreads / 32;
-  int g = (nslices + 2 * warps_per_cta - 1) / (2 * warps_per_cta);
+  int g = (nslices + warps_per_cta - 1) / warps_per_cta;
   if (g < 1) g = 1;
   if (g > kMaxCtas) g = kMaxCtas;
   return g;
+}
+
+static int spmv_flags(double alpha, double beta) {
+  int f = 0;
+  if (alpha == 0.0) f |= F_ALPHA_ZERO;
+  if (alpha == 1.0) f |= F_ALPHA_ONE;
+  if (beta == 0.0) f |= F_BETA_ZERO;
+  return f;
 }
 
 template <int B, typename V, typename A, int EPI>
@@ -385,8 +399,13 @@ static void launch_spmv(const Sell& m, const void* x, const void* y, void* z, do
   SellView<V> view{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
                    m.vals.as<V>()};
   EpiDev<A> e{(const A*)ep.aux0, (const A*)ep.aux1};
-  sell_spmv_kernel<B, V, A, EPI><<<spmv_grid(m.nslices), kThreads, 0, st>>>(
-      view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, guard, e, red);
+  const int flags = spmv_flags(alpha, beta);
+  if (red.w != nullptr)
+    sell_spmv_kernel<B, V, A, EPI, true><<<spmv_grid(m.nslices), kThreads, 0, st>>>(
+        view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+  else
+    sell_spmv_kernel<B, V, A, EPI, false><<<spmv_grid(m.nslices), kThreads, 0, st>>>(
+        view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
 }
 
 template <int B, typename V, typename A>
