@@ -61,6 +61,7 @@ struct SellView {
   const int64_t* slice_ptr;
   const int32_t* cols;
   const V* vals;
+  const int32_t* perm;  // stored row k is matrix row perm[k] (nullptr: identity)
 };
 
 // ---------------------------------------------------------------------------

@@ -44,6 +44,9 @@ struct Sell {
   DevBuf slice_ptr;  // int64[nslices + 1]
   DevBuf cols;       // int32[nent]
   DevBuf vals;       // vdtype[nent * B * B]
+  DevBuf perm;       // int32[nrow] when rows are stored sorted by length
+  int variant = 0;   // product kernel variant chosen by sell_autotune
+  int64_t nnz = 0;   // stored entries without padding
 };
 
 // Build options: output row k reads source row rows[k] (rows == nullptr:
@@ -61,6 +64,11 @@ struct SellBuild {
 int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,
                const void* val, int in_dtype, int out_dtype, const SellBuild& opt,
                cudaStream_t st);
+
+// Time the product kernel variants on `m` (vectors of dtype adtype) and keep
+// the fastest.  All variants sum each row in the same order, so the choice
+// never changes results.
+int sell_autotune(Sell& m, int adtype, cudaStream_t st);
 
 // Epilogues of the SELL product (see gbpc_sell.cu).
 enum EpiKind : int {

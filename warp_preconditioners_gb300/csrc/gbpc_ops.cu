@@ -347,6 +347,7 @@ extern "C" int gbpc_op_sparse(int nrow, int ncol, int block, const int32_t* offs
   op->vdtype = vector_dtype;
   rc = sell_build(op->m, nrow, ncol, block, offsets, columns, values, value_dtype, value_dtype,
                   SellBuild{}, st);
+  if (!rc) rc = sell_autotune(op->m, vector_dtype, st);
   if (!rc) rc = op->alias_scratch.alloc(dtype_size(vector_dtype) * std::max<int64_t>(op->rows, 1));
   if (rc) {
     delete op;
@@ -379,6 +380,8 @@ extern "C" int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int
   const int in = input_dtype(value_dtype);
   rc = sell_build(op->g, nrow, nrow, block, g_off, g_col, g_val, in, value_dtype, SellBuild{}, st);
   if (!rc) rc = sell_build(op->gt, nrow, nrow, block, gt_off, gt_col, gt_val, in, value_dtype, SellBuild{}, st);
+  if (!rc) rc = sell_autotune(op->g, vector_dtype, st);
+  if (!rc) rc = sell_autotune(op->gt, vector_dtype, st);
   if (!rc) rc = op->tmp.alloc(dtype_size(vector_dtype) * std::max<int64_t>(op->rows, 1));
   if (!rc) {
     cudaError_t e = cudaStreamSynchronize(st);
@@ -487,6 +490,8 @@ extern "C" int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* colum
   if ((rc = sell_build(op->fwd, n, nfree, 1, offsets, columns, values, dtype, dtype, fo, st))) return fail(rc);
   if ((rc = sell_build(op->bwd, nfree, n, 1, offsets, columns, values, dtype, dtype, bo, st))) return fail(rc);
   if ((rc = sell_build(op->bnd, n, n, 1, offsets, columns, values, dtype, dtype, bd, st))) return fail(rc);
+  if ((rc = sell_autotune(op->fwd, dtype, st))) return fail(rc);
+  if ((rc = sell_autotune(op->bwd, dtype, st))) return fail(rc);
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     gbpc_set_error_cuda(e, "sqlap setup", __FILE__, __LINE__);

@@ -8,9 +8,11 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
 
 #include "gbpc_common.cuh"
 #include "gbpc_internal.h"
@@ -85,30 +87,60 @@ __device__ __forceinline__ bool keep_entry(int part, int src_row, int c) {
   return part == 0 || (part == 1 && c < src_row) || (part == 2 && c > src_row);
 }
 
-__global__ void sell_width_kernel(int nrow, int nslices, const int32_t* __restrict__ off,
-                                  const int32_t* __restrict__ col, const int32_t* rows,
-                                  const int32_t* colmap, int part, int64_t* slice_entries) {
+// Stored entries of each output row after the build filters.
+__global__ void sell_length_kernel(int nrow, const int32_t* __restrict__ off,
+                                   const int32_t* __restrict__ col, const int32_t* rows,
+                                   const int32_t* colmap, int part, int32_t* len) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrow) return;
+  const int src = rows ? rows[r] : r;
+  int count = 0;
+  if (colmap == nullptr && part == 0) {
+    count = off[src + 1] - off[src];
+  } else {
+    for (int e = off[src]; e < off[src + 1]; ++e) {
+      const int c = col[e];
+      if (!keep_entry(part, src, c)) continue;
+      if (colmap && colmap[c] < 0) continue;
+      ++count;
+    }
+  }
+  len[r] = count;
+}
+
+// Rows ordered by decreasing length inside windows of `window` rows (a stable
+// counting sort per window, one thread per window), so that each 32-row slice
+// holds rows of similar length and padding stays small.
+__global__ void window_sort_kernel(int nrow, int window, int maxlen, const int32_t* __restrict__ len,
+                                   int32_t* perm) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lo = w * window;
+  if (lo >= nrow) return;
+  const int hi = min(nrow, lo + window);
+  int pos = lo;
+  for (int l = maxlen; l >= 0; --l)
+    for (int r = lo; r < hi; ++r)
+      if (len[r] == l) perm[pos++] = r;
+}
+
+__global__ void sell_width_kernel(int nrow, int nslices, const int32_t* __restrict__ len,
+                                  const int32_t* perm, int64_t* slice_entries) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nslices) return;
   int width = 0;
   for (int l = 0; l < kSlice; ++l) {
-    const int r = s * kSlice + l;
-    if (r >= nrow) break;
-    const int src = rows ? rows[r] : r;
-    int count = 0;
-    if (rows == nullptr && colmap == nullptr && part == 0) {
-      count = off[src + 1] - off[src];
-    } else {
-      for (int e = off[src]; e < off[src + 1]; ++e) {
-        const int c = col[e];
-        if (!keep_entry(part, src, c)) continue;
-        if (colmap && colmap[c] < 0) continue;
-        ++count;
-      }
-    }
-    width = max(width, count);
+    const int k = s * kSlice + l;
+    if (k >= nrow) break;
+    width = max(width, len[perm ? perm[k] : k]);
   }
   slice_entries[s] = (int64_t)width * kSlice;
+}
+
+__global__ void max_kernel(int n, const int32_t* __restrict__ v, int32_t* out) {
+  int m = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = max(m, v[i]);
+  atomicMax(out, m);
 }
 
 // Exclusive scan of int64 counts by a single CTA (setup only).
@@ -156,17 +188,19 @@ template <typename VI, typename VO>
 __global__ void sell_fill_kernel(int nrow, int nslices, int B, const int32_t* __restrict__ off,
                                  const int32_t* __restrict__ col, const VI* __restrict__ val,
                                  const int32_t* rows, const int32_t* colmap, int part,
-                                 const VI* row_scale, const int64_t* __restrict__ slice_ptr,
-                                 int32_t* cols_out, VO* vals_out) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = r / kSlice;
+                                 const VI* row_scale, const int32_t* perm,
+                                 const int64_t* __restrict__ slice_ptr, int32_t* cols_out,
+                                 VO* vals_out) {
+  const int k_row = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = k_row / kSlice;
   if (s >= nslices) return;
-  const int lane = r % kSlice;
+  const int lane = k_row % kSlice;
   const int64_t base = slice_ptr[s];
   const int width = (int)((slice_ptr[s + 1] - base) / kSlice);
   const int BB = B * B;
   int k = 0;
-  if (r < nrow) {
+  if (k_row < nrow) {
+    const int r = perm ? perm[k_row] : k_row;
     const int src = rows ? rows[r] : r;
     for (int e = off[src]; e < off[src + 1]; ++e) {
       int c = col[e];
@@ -199,8 +233,14 @@ static void launch_fill(const Sell& s, int B, const int32_t* off, const int32_t*
   const int threads = s.nslices * kSlice;
   sell_fill_kernel<VI, VO><<<grid_for(threads, kThreads), kThreads, 0, st>>>(
       s.nrow, s.nslices, B, off, col, (const VI*)val, opt.rows, opt.colmap, opt.part,
-      (const VI*)opt.row_scale, s.slice_ptr.as<int64_t>(), s.cols.as<int32_t>(), s.vals.as<VO>());
+      (const VI*)opt.row_scale, s.perm.p ? s.perm.as<int32_t>() : nullptr,
+      s.slice_ptr.as<int64_t>(), s.cols.as<int32_t>(), s.vals.as<VO>());
 }
+
+// Rows are sorted by length inside windows when the plain layout would pad
+// more than this fraction.
+constexpr double kSortPadding = 0.10;
+constexpr int kSortWindow = 256;
 
 int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,
                const void* val, int in_dtype, int out_dtype, const SellBuild& opt,
@@ -219,19 +259,57 @@ int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const
   s.B = B;
   s.vdtype = out_dtype;
   s.nslices = (nrow_out + kSlice - 1) / kSlice;
+  s.perm.release();
   int rc = s.slice_ptr.alloc(sizeof(int64_t) * (s.nslices + 1));
   if (rc) return rc;
-  DevBuf counts;
+  DevBuf counts, len, scratch;
   if ((rc = counts.alloc(sizeof(int64_t) * (s.nslices + 1)))) return rc;
-  if (s.nslices > 0) {
+  if ((rc = len.alloc(sizeof(int32_t) * (nrow_out + 1)))) return rc;
+  if ((rc = scratch.alloc(sizeof(int32_t) * 2))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(scratch.p, 0, sizeof(int32_t) * 2, st));
+  if (nrow_out > 0) {
+    sell_length_kernel<<<grid_for(nrow_out, kThreads), kThreads, 0, st>>>(
+        nrow_out, off, col, opt.rows, opt.colmap, opt.part, len.as<int32_t>());
     sell_width_kernel<<<grid_for(s.nslices, kThreads), kThreads, 0, st>>>(
-        nrow_out, s.nslices, off, col, opt.rows, opt.colmap, opt.part, counts.as<int64_t>());
+        nrow_out, s.nslices, len.as<int32_t>(), nullptr, counts.as<int64_t>());
   }
   scan_i64_kernel<<<1, 1024, 0, st>>>(counts.as<int64_t>(), s.slice_ptr.as<int64_t>(), s.nslices);
   GBPC_CUDA_TRY(cudaGetLastError());
+  if (nrow_out > 0)
+    max_kernel<<<std::min(grid_for(nrow_out, kThreads), 1024), kThreads, 0, st>>>(
+        nrow_out, len.as<int32_t>(), scratch.as<int32_t>());
+  GBPC_CUDA_TRY(cudaGetLastError());
+  int32_t maxlen = 0;
   GBPC_CUDA_TRY(cudaMemcpyAsync(&s.nent, s.slice_ptr.as<int64_t>() + s.nslices, sizeof(int64_t),
                                 cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaMemcpyAsync(&maxlen, scratch.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  // Try rows sorted by length inside windows; keep that layout when it saves
+  // more than kSortPadding of the stored entries.
+  if (nrow_out > kSlice && maxlen > 0) {
+    DevBuf perm, counts2, ptr2;
+    if ((rc = perm.alloc(sizeof(int32_t) * nrow_out))) return rc;
+    if ((rc = counts2.alloc(sizeof(int64_t) * (s.nslices + 1)))) return rc;
+    if ((rc = ptr2.alloc(sizeof(int64_t) * (s.nslices + 1)))) return rc;
+    const int nwin = (nrow_out + kSortWindow - 1) / kSortWindow;
+    window_sort_kernel<<<grid_for(nwin, 128), 128, 0, st>>>(nrow_out, kSortWindow, maxlen,
+                                                           len.as<int32_t>(), perm.as<int32_t>());
+    sell_width_kernel<<<grid_for(s.nslices, kThreads), kThreads, 0, st>>>(
+        nrow_out, s.nslices, len.as<int32_t>(), perm.as<int32_t>(), counts2.as<int64_t>());
+    scan_i64_kernel<<<1, 1024, 0, st>>>(counts2.as<int64_t>(), ptr2.as<int64_t>(), s.nslices);
+    GBPC_CUDA_TRY(cudaGetLastError());
+    int64_t nent2 = 0;
+    GBPC_CUDA_TRY(cudaMemcpyAsync(&nent2, ptr2.as<int64_t>() + s.nslices, sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, st));
+    GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+    if ((double)nent2 < (double)s.nent * (1.0 - kSortPadding)) {
+      std::swap(s.perm.p, perm.p);
+      std::swap(s.perm.bytes, perm.bytes);
+      std::swap(s.slice_ptr.p, ptr2.p);
+      std::swap(s.slice_ptr.bytes, ptr2.bytes);
+      s.nent = nent2;
+    }
+  }
   if ((rc = s.cols.alloc(sizeof(int32_t) * s.nent))) return rc;
   if ((rc = s.vals.alloc(dtype_size(out_dtype) * s.nent * B * B))) return rc;
   if (s.nslices > 0) {
@@ -248,207 +326,28 @@ int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const
     }
   }
   GBPC_CUDA_TRY(cudaGetLastError());
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
   return GBPC_OK;
 }
 
 // ---------------------------------------------------------------------------
-// The sliced product.
-//
-// One warp per slice, slices distributed over a grid that fills the GPU.  For
-// each chunk of entries the warp first issues every column-index load, then
-// every value load and x gather, then the FMAs, so each lane keeps a whole
-// chunk of independent memory requests in flight.  alpha/beta tests are
-// uniform integer flags computed on the host: FP64 compares would take FP64
-// issue slots, the scarce resource on this GPU.
+// Product entry point (kernels in gbpc_spmv.cuh, instantiated per vector type
+// in gbpc_spmv_f64.cu and gbpc_spmv_f32.cu).
 
-template <typename A>
-struct EpiDev {
-  const A* aux0;
-  const A* aux1;
-};
-
-template <typename A>
-__device__ __forceinline__ A fma_t(A a, A b, A c);
-template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
-template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
-
-enum SpmvFlags : int { F_ALPHA_ZERO = 1, F_ALPHA_ONE = 2, F_BETA_ZERO = 4 };
-
-template <int B> struct Chunk { static constexpr int value = 8; };
-template <> struct Chunk<2> { static constexpr int value = 4; };
-template <> struct Chunk<3> { static constexpr int value = 2; };
-template <> struct Chunk<4> { static constexpr int value = 2; };
-
-template <int B, typename V, typename A, int EPI, bool DOT>
-__global__ void __launch_bounds__(kThreads)
-sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
-                 const int* guard, EpiDev<A> ep, Reduction red) {
-  if (guard_off(guard)) return;
-  constexpr int BB = B * B;
-  constexpr int CH = Chunk<B>::value;
-  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
-  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
-  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
-  const int lane = threadIdx.x & 31;
-  const int warps_total = gridDim.x * (kThreads / 32);
-  double dot_part = 0.0;
-  for (int s = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); s < m.nslices; s += warps_total) {
-    const int row = s * kSlice + lane;
-    const int64_t base = __ldg(m.slice_ptr + s);
-    const int width = (int)((__ldg(m.slice_ptr + s + 1) - base) >> 5);
-    A acc[B];
-#pragma unroll
-    for (int r = 0; r < B; ++r) acc[r] = A(0);
-    if (run) {
-      const int32_t* cp = m.cols + base + lane;
-      const V* vp = m.vals + base * BB + lane;
-      for (int k0 = 0; k0 < width; k0 += CH) {
-        int c[CH];
-#pragma unroll
-        for (int j = 0; j < CH; ++j)
-          c[j] = (k0 + j < width) ? __ldg(cp + (int64_t)(k0 + j) * kSlice) : -1;
-        A xv[CH][B];
-        V vv[CH][BB];
-#pragma unroll
-        for (int j = 0; j < CH; ++j) {
-#pragma unroll
-          for (int q = 0; q < B; ++q) xv[j][q] = (c[j] >= 0) ? __ldg(x + (int64_t)c[j] * B + q) : A(0);
-#pragma unroll
-          for (int q = 0; q < BB; ++q)
-            vv[j][q] = (k0 + j < width) ? __ldg(vp + ((int64_t)(k0 + j) * BB + q) * kSlice)
-                                        : static_cast<V>(0.0f);
-        }
-#pragma unroll
-        for (int j = 0; j < CH; ++j) {
-          if (k0 + j < width) {  // uniform across the warp
-#pragma unroll
-            for (int r = 0; r < B; ++r)
-#pragma unroll
-              for (int q = 0; q < B; ++q) acc[r] = fma_t<A>(widen<A, V>(vv[j][r * B + q]), xv[j][q], acc[r]);
-          }
-        }
-      }
-    }
-    if (row < m.nrow) {
-      A out[B];
-#pragma unroll
-      for (int r = 0; r < B; ++r) {
-        const int64_t idx = (int64_t)row * B + r;
-        if (EPI == EPI_AXPBY) {
-          A v = alpha_one ? acc[r] : alpha * acc[r];
-          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
-          out[r] = v;
-        } else if (EPI == EPI_SQLAP_BWD) {
-          A v = A(0);
-          if (run) {
-            v = fma_t<A>(ep.aux0[idx], ep.aux1[idx], acc[r]);
-            if (!alpha_one) v = alpha * v;
-          }
-          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
-          out[r] = v;
-        } else if (EPI == EPI_SQLAP_FWD) {
-          out[r] = ep.aux0[idx] * acc[r];
-        } else {
-          out[r] = ep.aux0[idx] - acc[r];
-        }
-      }
-      if (EPI == EPI_TRI_UPPER) {
-        A t[B];
-#pragma unroll
-        for (int r = 0; r < B; ++r) {
-          A s2 = A(0);
-#pragma unroll
-          for (int q = 0; q < B; ++q) s2 = fma_t<A>(ep.aux1[(int64_t)row * BB + r * B + q], out[q], s2);
-          t[r] = s2;
-        }
-#pragma unroll
-        for (int r = 0; r < B; ++r) out[r] = t[r];
-      }
-#pragma unroll
-      for (int r = 0; r < B; ++r) {
-        const int64_t idx = (int64_t)row * B + r;
-        z[idx] = out[r];
-        if (DOT) dot_part = fma((double)out[r], red.w[idx], dot_part);
-      }
-    }
-  }
-  if (DOT) reduce_and_finalize(red, dot_part);
-}
-
-static int spmv_grid(int nslices) {
-  // One slice per warp, at most one wave of resident CTAs.
-  const int warps_per_cta = kThreads / 32;
-  int g = (nslices + warps_per_cta - 1) / warps_per_cta;
-  if (g < 1) g = 1;
-  if (g > kMaxCtas) g = kMaxCtas;
-  return g;
-}
-
-static int spmv_flags(double alpha, double beta) {
-  int f = 0;
-  if (alpha == 0.0) f |= F_ALPHA_ZERO;
-  if (alpha == 1.0) f |= F_ALPHA_ONE;
-  if (beta == 0.0) f |= F_BETA_ZERO;
-  return f;
-}
-
-template <int B, typename V, typename A, int EPI>
-static void launch_spmv(const Sell& m, const void* x, const void* y, void* z, double alpha,
-                        double beta, const int* guard, const EpiHost& ep, const Reduction& red,
-                        cudaStream_t st) {
-  SellView<V> view{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
-                   m.vals.as<V>()};
-  EpiDev<A> e{(const A*)ep.aux0, (const A*)ep.aux1};
-  const int flags = spmv_flags(alpha, beta);
-  if (red.w != nullptr)
-    sell_spmv_kernel<B, V, A, EPI, true><<<spmv_grid(m.nslices), kThreads, 0, st>>>(
-        view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
-  else
-    sell_spmv_kernel<B, V, A, EPI, false><<<spmv_grid(m.nslices), kThreads, 0, st>>>(
-        view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
-}
-
-template <int B, typename V, typename A>
-static int dispatch_epi(const Sell& m, const void* x, const void* y, void* z, double alpha,
-                        double beta, const int* guard, const EpiHost& ep, const Reduction& red,
-                        cudaStream_t st) {
-  switch (ep.kind) {
-    case EPI_AXPBY: launch_spmv<B, V, A, EPI_AXPBY>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-    case EPI_TRI_LOWER: launch_spmv<B, V, A, EPI_TRI_LOWER>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-    case EPI_TRI_UPPER: launch_spmv<B, V, A, EPI_TRI_UPPER>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-    case EPI_SQLAP_FWD:
-      if (B != 1) return GBPC_ERR_ARG;
-      launch_spmv<1, V, A, EPI_SQLAP_FWD>(m, x, y, z, alpha, beta, guard, ep, red, st);
-      break;
-    case EPI_SQLAP_BWD:
-      if (B != 1) return GBPC_ERR_ARG;
-      launch_spmv<1, V, A, EPI_SQLAP_BWD>(m, x, y, z, alpha, beta, guard, ep, red, st);
-      break;
-    default: return GBPC_ERR_ARG;
-  }
-  return GBPC_OK;
-}
-
-template <int B, typename A>
-static int dispatch_v(const Sell& m, const void* x, const void* y, void* z, double alpha,
-                      double beta, const int* guard, const EpiHost& ep, const Reduction& red,
-                      cudaStream_t st) {
-  switch (m.vdtype) {
-    case GBPC_F64:
-      if (sizeof(A) == 4) break;  // float64 storage needs float64 vectors
-      return dispatch_epi<B, double, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
-    case GBPC_F32: return dispatch_epi<B, float, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
-    case GBPC_BF16: return dispatch_epi<B, __nv_bfloat16, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
-  }
-  gbpc_set_error("unsupported storage/vector dtype combination %d/%d", m.vdtype, (int)sizeof(A));
-  return GBPC_ERR_ARG;
-}
+int spmv_f64(const Sell& m, const void* x, const void* y, void* z, double alpha, double beta,
+             const int* guard, const EpiHost& ep, const Reduction& red, cudaStream_t st);
+int spmv_f32(const Sell& m, const void* x, const void* y, void* z, double alpha, double beta,
+             const int* guard, const EpiHost& ep, const Reduction& red, cudaStream_t st);
 
 int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, double alpha,
               double beta, const int* guard, const EpiHost& ep, const DotSpec* dot,
               cudaStream_t st) {
   Reduction red{};
   if (dot != nullptr && dot->w != nullptr) {
+    if (adtype != GBPC_F64) {
+      gbpc_set_error("fused dot products need float64 vectors");
+      return GBPC_ERR_ARG;
+    }
     red.w = dot->w;
     red.partials = dot->rb->partials.as<double>();
     red.counter = dot->rb->counter.as<unsigned int>();
@@ -457,30 +356,58 @@ int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, 
     red.out = dot->out;
   }
   int rc;
-  if (adtype == GBPC_F64) {
-    switch (m.B) {
-      case 1: rc = dispatch_v<1, double>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      case 2: rc = dispatch_v<2, double>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      case 3: rc = dispatch_v<3, double>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      case 4: rc = dispatch_v<4, double>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      default: rc = GBPC_ERR_ARG;
-    }
-  } else if (adtype == GBPC_F32) {
-    if (dot != nullptr && dot->w != nullptr) {
-      gbpc_set_error("fused dot products need float64 vectors");
-      return GBPC_ERR_ARG;
-    }
-    switch (m.B) {
-      case 1: rc = dispatch_v<1, float>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      case 2: rc = dispatch_v<2, float>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      case 3: rc = dispatch_v<3, float>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      case 4: rc = dispatch_v<4, float>(m, x, y, z, alpha, beta, guard, ep, red, st); break;
-      default: rc = GBPC_ERR_ARG;
-    }
-  } else {
+  if (adtype == GBPC_F64) rc = spmv_f64(m, x, y, z, alpha, beta, guard, ep, red, st);
+  else if (adtype == GBPC_F32) rc = spmv_f32(m, x, y, z, alpha, beta, guard, ep, red, st);
+  else {
     gbpc_set_error("vector dtype must be float64 or float32");
     return GBPC_ERR_ARG;
   }
+  if (rc) return rc;
+  GBPC_CUDA_TRY(cudaGetLastError());
+  return GBPC_OK;
+}
+
+// Kernel variants timed by the autotuner (scalar rows; must match
+// launch_variant in gbpc_spmv.cuh).
+constexpr int kNumVariants = 3;
+
+int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
+  if (m.B != 1 || m.nslices == 0) {
+    m.variant = 0;
+    return GBPC_OK;
+  }
+  const size_t vs = dtype_size(adtype);
+  DevBuf x, z;
+  int rc;
+  if ((rc = x.alloc(vs * std::max(m.ncol, 1)))) return rc;
+  if ((rc = z.alloc(vs * std::max(m.nrow, 1)))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(x.p, 0, vs * std::max(m.ncol, 1), st));
+  cudaEvent_t e0, e1;
+  GBPC_CUDA_TRY(cudaEventCreate(&e0));
+  GBPC_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_v = 0;
+  for (int v = 0; v < kNumVariants; ++v) {
+    m.variant = v;
+    for (int w = 0; w < 2; ++w)
+      if ((rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st)))
+        break;
+    cudaEventRecord(e0, st);
+    for (int w = 0; w < 5 && !rc; ++w)
+      rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);
+    cudaEventRecord(e1, st);
+    if (rc) break;
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  m.variant = best_v;
   if (rc) return rc;
   GBPC_CUDA_TRY(cudaGetLastError());
   return GBPC_OK;

@@ -1,0 +1,273 @@
+// The sliced sparse product (SELL-32) shared by the per-vector-type
+// translation units gbpc_spmv_f64.cu and gbpc_spmv_f32.cu.
+#pragma once
+
+#include <type_traits>
+
+#include "gbpc_common.cuh"
+#include "gbpc_internal.h"
+
+namespace gbpc {
+
+// ---------------------------------------------------------------------------
+// The sliced product.
+//
+// One warp per slice, slices distributed over a grid that fills the GPU.  For
+// each chunk of entries the warp first issues every column-index load, then
+// every value load and x gather, then the FMAs, so each lane keeps a whole
+// chunk of independent memory requests in flight.  alpha/beta tests are
+// uniform integer flags computed on the host: FP64 compares would take FP64
+// issue slots, the scarce resource on this GPU.
+
+template <typename A>
+struct EpiDev {
+  const A* aux0;
+  const A* aux1;
+};
+
+template <typename A>
+__device__ __forceinline__ A fma_t(A a, A b, A c);
+template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+enum SpmvFlags : int { F_ALPHA_ZERO = 1, F_ALPHA_ONE = 2, F_BETA_ZERO = 4 };
+
+template <int B> struct Chunk { static constexpr int value = 8; };
+template <> struct Chunk<2> { static constexpr int value = 4; };
+template <> struct Chunk<3> { static constexpr int value = 2; };
+template <> struct Chunk<4> { static constexpr int value = 2; };
+
+template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
+                 const int* guard, EpiDev<A> ep, Reduction red) {
+  if (guard_off(guard)) return;
+  constexpr int BB = B * B;
+  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  double dot_part = 0.0;
+  for (int s = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); s < m.nslices; s += warps_total) {
+    const int row = s * kSlice + lane;
+    const int64_t base = __ldg(m.slice_ptr + s);
+    const int width = (int)((__ldg(m.slice_ptr + s + 1) - base) >> 5);
+    A acc[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) acc[r] = A(0);
+    if (run) {
+      const int32_t* cp = m.cols + base + lane;
+      const V* vp = m.vals + base * BB + lane;
+      for (int k0 = 0; k0 < width; k0 += CH) {
+        int c[CH];
+#pragma unroll
+        for (int j = 0; j < CH; ++j)
+          c[j] = (k0 + j < width) ? __ldg(cp + (int64_t)(k0 + j) * kSlice) : -1;
+        A xv[CH][B];
+        V vv[CH][BB];
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+#pragma unroll
+          for (int q = 0; q < B; ++q) xv[j][q] = (c[j] >= 0) ? __ldg(x + (int64_t)c[j] * B + q) : A(0);
+#pragma unroll
+          for (int q = 0; q < BB; ++q)
+            vv[j][q] = (k0 + j < width) ? __ldg(vp + ((int64_t)(k0 + j) * BB + q) * kSlice)
+                                        : static_cast<V>(0.0f);
+        }
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          if (k0 + j < width) {  // uniform across the warp
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+              for (int q = 0; q < B; ++q) acc[r] = fma_t<A>(widen<A, V>(vv[j][r * B + q]), xv[j][q], acc[r]);
+          }
+        }
+      }
+    }
+    if (row < m.nrow) {
+      const int orow = m.perm ? __ldg(m.perm + row) : row;
+      A out[B];
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const int64_t idx = (int64_t)orow * B + r;
+        if (EPI == EPI_AXPBY) {
+          A v = alpha_one ? acc[r] : alpha * acc[r];
+          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
+          out[r] = v;
+        } else if (EPI == EPI_SQLAP_BWD) {
+          A v = A(0);
+          if (run) {
+            v = fma_t<A>(ep.aux0[idx], ep.aux1[idx], acc[r]);
+            if (!alpha_one) v = alpha * v;
+          }
+          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
+          out[r] = v;
+        } else if (EPI == EPI_SQLAP_FWD) {
+          out[r] = ep.aux0[idx] * acc[r];
+        } else {
+          out[r] = ep.aux0[idx] - acc[r];
+        }
+      }
+      if (EPI == EPI_TRI_UPPER) {
+        A t[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+          A s2 = A(0);
+#pragma unroll
+          for (int q = 0; q < B; ++q) s2 = fma_t<A>(ep.aux1[(int64_t)orow * BB + r * B + q], out[q], s2);
+          t[r] = s2;
+        }
+#pragma unroll
+        for (int r = 0; r < B; ++r) out[r] = t[r];
+      }
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const int64_t idx = (int64_t)orow * B + r;
+        z[idx] = out[r];
+        if (DOT) dot_part = fma((double)out[r], red.w[idx], dot_part);
+      }
+    }
+  }
+  if (DOT) reduce_and_finalize(red, dot_part);
+}
+
+// Launch configuration of a variant: CTAs resident per SM times SMs, with
+// slices spread over the warps by a grid stride.
+static int spmv_grid(int nslices, int minb) {
+  const int warps_per_cta = kThreads / 32;
+  int g = (nslices + warps_per_cta - 1) / warps_per_cta;
+  const int cap = 152 * minb;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return g;
+}
+
+static int spmv_flags(double alpha, double beta) {
+  int f = 0;
+  if (alpha == 0.0) f |= F_ALPHA_ZERO;
+  if (alpha == 1.0) f |= F_ALPHA_ONE;
+  if (beta == 0.0) f |= F_BETA_ZERO;
+  return f;
+}
+
+// Product kernel variants for scalar rows: (entries loaded per chunk,
+// minimum resident CTAs per SM).  Blocked rows use one variant.
+constexpr int kNumVariants = 3;
+
+template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
+static void launch_one(const SellView<V>& view, const void* x, const void* y, void* z,
+                       double alpha, double beta, int flags, const int* guard, const EpiDev<A>& e,
+                       const Reduction& red, int nslices, cudaStream_t st) {
+  sell_spmv_kernel<B, V, A, EPI, DOT, CH, MINB><<<spmv_grid(nslices, MINB), kThreads, 0, st>>>(
+      view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+}
+
+template <int B, typename V, typename A, int EPI, bool DOT>
+static void launch_variant(int variant, const SellView<V>& view, const void* x, const void* y,
+                           void* z, double alpha, double beta, int flags, const int* guard,
+                           const EpiDev<A>& e, const Reduction& red, int nslices,
+                           cudaStream_t st) {
+  if (B == 1) {
+    switch (variant) {
+      case 1:
+        launch_one<B, V, A, EPI, DOT, 16, 4>(view, x, y, z, alpha, beta, flags, guard, e, red,
+                                             nslices, st);
+        return;
+      case 2:
+        launch_one<B, V, A, EPI, DOT, 4, 8>(view, x, y, z, alpha, beta, flags, guard, e, red,
+                                            nslices, st);
+        return;
+      default:
+        break;
+    }
+  }
+  launch_one<B, V, A, EPI, DOT, Chunk<B>::value, 8>(view, x, y, z, alpha, beta, flags, guard, e,
+                                                    red, nslices, st);
+}
+
+template <int B, typename V, typename A, int EPI>
+static void launch_spmv(const Sell& m, const void* x, const void* y, void* z, double alpha,
+                        double beta, const int* guard, const EpiHost& ep, const Reduction& red,
+                        cudaStream_t st) {
+  SellView<V> view{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
+                   m.vals.as<V>(), m.perm.p ? m.perm.as<int32_t>() : nullptr};
+  EpiDev<A> e{(const A*)ep.aux0, (const A*)ep.aux1};
+  const int flags = spmv_flags(alpha, beta);
+  if (red.w != nullptr)
+    launch_variant<B, V, A, EPI, true>(m.variant, view, x, y, z, alpha, beta, flags, guard, e,
+                                       red, m.nslices, st);
+  else
+    launch_variant<B, V, A, EPI, false>(m.variant, view, x, y, z, alpha, beta, flags, guard, e,
+                                        red, m.nslices, st);
+}
+
+// Epilogue dispatch.  Triangular-sweep epilogues exist only for V == A,
+// the factored-operator epilogue only for scalar rows.
+template <int B, typename V, typename A>
+static int dispatch_epi(const Sell& m, const void* x, const void* y, void* z, double alpha,
+                        double beta, const int* guard, const EpiHost& ep, const Reduction& red,
+                        cudaStream_t st) {
+  switch (ep.kind) {
+    case EPI_AXPBY:
+      launch_spmv<B, V, A, EPI_AXPBY>(m, x, y, z, alpha, beta, guard, ep, red, st);
+      return GBPC_OK;
+    case EPI_TRI_LOWER:
+    case EPI_TRI_UPPER:
+      if constexpr (std::is_same<V, A>::value) {
+        if (ep.kind == EPI_TRI_LOWER)
+          launch_spmv<B, V, A, EPI_TRI_LOWER>(m, x, y, z, alpha, beta, guard, ep, red, st);
+        else
+          launch_spmv<B, V, A, EPI_TRI_UPPER>(m, x, y, z, alpha, beta, guard, ep, red, st);
+        return GBPC_OK;
+      }
+      break;
+    case EPI_SQLAP_BWD:
+      if constexpr (B == 1 && std::is_same<V, A>::value) {
+        launch_spmv<1, V, A, EPI_SQLAP_BWD>(m, x, y, z, alpha, beta, guard, ep, red, st);
+        return GBPC_OK;
+      }
+      break;
+    default:
+      break;
+  }
+  gbpc_set_error("unsupported product epilogue %d for this block size / dtype", ep.kind);
+  return GBPC_ERR_ARG;
+}
+
+// All products whose vectors have type A.
+template <typename A>
+static int spmv_dispatch(const Sell& m, const void* x, const void* y, void* z, double alpha,
+                         double beta, const int* guard, const EpiHost& ep, const Reduction& red,
+                         cudaStream_t st) {
+  auto by_block = [&](auto vtag) -> int {
+    using V = decltype(vtag);
+    switch (m.B) {
+      case 1: return dispatch_epi<1, V, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
+      case 2: return dispatch_epi<2, V, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
+      case 3: return dispatch_epi<3, V, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
+      case 4: return dispatch_epi<4, V, A>(m, x, y, z, alpha, beta, guard, ep, red, st);
+    }
+    gbpc_set_error("block size must be 1..4");
+    return GBPC_ERR_ARG;
+  };
+  switch (m.vdtype) {
+    case GBPC_F64:
+      if constexpr (std::is_same<A, double>::value) return by_block(double{});
+      break;
+    case GBPC_F32:
+      return by_block(float{});
+    case GBPC_BF16:
+      return by_block(__nv_bfloat16{});
+  }
+  gbpc_set_error("unsupported storage/vector dtype combination %d/%d", m.vdtype, (int)sizeof(A));
+  return GBPC_ERR_ARG;
+}
+
+int spmv_f64(const Sell& m, const void* x, const void* y, void* z, double alpha, double beta,
+             const int* guard, const EpiHost& ep, const Reduction& red, cudaStream_t st);
+int spmv_f32(const Sell& m, const void* x, const void* y, void* z, double alpha, double beta,
+             const int* guard, const EpiHost& ep, const Reduction& red, cudaStream_t st);
+
+}  // namespace gbpc
