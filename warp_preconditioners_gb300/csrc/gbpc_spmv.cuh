@@ -53,14 +53,9 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
     const int row = s * kSlice + lane;
     const int64_t base = __ldg(m.slice_ptr + s);
     const int width = (int)((__ldg(m.slice_ptr + s + 1) - base) >> 5);
-    // Two accumulators (even / odd entries) halve the dependent FMA chain;
-    // every variant uses the same split, so all variants agree bit for bit.
-    A acc[B], acc2[B];
+    A acc[B];
 #pragma unroll
-    for (int r = 0; r < B; ++r) {
-      acc[r] = A(0);
-      acc2[r] = A(0);
-    }
+    for (int r = 0; r < B; ++r) acc[r] = A(0);
     if (run) {
       const int32_t* cp = m.cols + base + lane;
       const V* vp = m.vals + base * BB + lane;
@@ -86,17 +81,10 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
 #pragma unroll
             for (int r = 0; r < B; ++r)
 #pragma unroll
-              for (int q = 0; q < B; ++q) {
-                if (j % 2 == 0)
-                  acc[r] = fma_t<A>(widen<A, V>(vv[j][r * B + q]), xv[j][q], acc[r]);
-                else
-                  acc2[r] = fma_t<A>(widen<A, V>(vv[j][r * B + q]), xv[j][q], acc2[r]);
-              }
+              for (int q = 0; q < B; ++q) acc[r] = fma_t<A>(widen<A, V>(vv[j][r * B + q]), xv[j][q], acc[r]);
           }
         }
       }
-#pragma unroll
-      for (int r = 0; r < B; ++r) acc[r] = acc[r] + acc2[r];
     }
     if (row < m.nrow) {
       const int orow = m.perm ? __ldg(m.perm + row) : row;
