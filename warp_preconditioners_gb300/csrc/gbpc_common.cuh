@@ -24,7 +24,12 @@
 namespace gbpc {
 
 constexpr int kSlice = 32;     // rows per SELL slice (one warp)
-constexpr int kThreads = 256;  // threads per CTA for streaming kernels
+constexpr int kThreads = 1024;  // threads per CTA for streaming kernels
+// Resident 1024-thread CTAs per SM for kernels within 32 registers per thread;
+// streaming grids are capped at this many CTAs per SM so reductions combine
+// few partial sums.
+constexpr int kCtasPerSm = 2;
+constexpr int kSms = 152;
 
 // ---------------------------------------------------------------------------
 // Value conversion helpers.
@@ -111,16 +116,27 @@ __device__ __forceinline__ bool guard_off(const int* guard) {
 }
 
 // Sum of one double per thread over a CTA of kThreads threads with few FP64
-// instructions: transpose through shared memory so warp 0 adds 8 values per
-// lane with full lanes, then a 5-step shuffle tree.  Result valid in thread 0.
+// instructions: transpose through shared memory so warp 0 adds kThreads/32
+// values per lane with full lanes, then a 5-step shuffle tree.  Result valid
+// in thread 0.
 __device__ __forceinline__ double block_sum(double v, double* smem /*kThreads*/) {
+  static_assert(kThreads % 128 == 0, "block_sum expects a multiple of 128 threads");
   smem[threadIdx.x] = v;
+  __syncthreads();
+  // 128 threads add kThreads/128 values each (each reads only its own
+  // column of smem before writing its own slot), then warp 0 adds 4 values
+  // per lane and finishes with a shuffle tree.
+  if (threadIdx.x < 128) {
+    double s = smem[threadIdx.x];
+#pragma unroll
+    for (int k = 1; k < kThreads / 128; ++k) s += smem[threadIdx.x + 128 * k];
+    smem[threadIdx.x] = s;
+  }
   __syncthreads();
   double s = 0.0;
   if (threadIdx.x < 32) {
-    s = smem[threadIdx.x];
-#pragma unroll
-    for (int k = 1; k < kThreads / 32; ++k) s += smem[threadIdx.x + 32 * k];
+    s = smem[threadIdx.x] + smem[threadIdx.x + 32];
+    s += smem[threadIdx.x + 64] + smem[threadIdx.x + 96];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   }

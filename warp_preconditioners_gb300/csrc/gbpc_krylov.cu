@@ -36,7 +36,7 @@ __device__ __forceinline__ bool inactive(const KrylovScalars* ks) {
 }
 
 // x += alpha p; r -= alpha Ap; reduce r.r
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const double* p,
                  const double* Ap, Reduction red) {
   if (inactive(ks)) return;
@@ -53,7 +53,7 @@ cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const doubl
 }
 
 // x += alpha p; r -= alpha Ap; z -= alpha y; reduce r.r
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, const double* p,
                  const double* Ap, const double* y, Reduction red) {
   if (inactive(ks)) return;
@@ -71,7 +71,7 @@ cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, 
 }
 
 // p = z + beta p  (and q = w + beta q when q != nullptr)
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, const double* w,
             double* q) {
   if (inactive(ks)) return;
@@ -84,7 +84,7 @@ xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, cons
 }
 
 // dot(a, b) into the reduction's finalize action (initialisation only).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 dot_kernel(int64_t n, const double* a, const double* b, Reduction red) {
   double part = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
@@ -110,7 +110,7 @@ __global__ void copy_outputs_kernel(const KrylovScalars* ks, int32_t* nit, doubl
   if (atol_sq) *atol_sq = ks->atol_sq;
 }
 
-int vec_grid(int64_t n) { return std::min<int64_t>(grid_for(n, kThreads), kMaxCtas); }
+int vec_grid(int64_t n) { return std::min<int64_t>(grid_for(n, kThreads), kSms * kCtasPerSm); }
 
 }  // namespace
 
@@ -344,7 +344,7 @@ struct Solver {
 };
 
 // Identity preconditioner helper (defined here to keep the reduction local).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 copy_dot_kernel(int64_t n, const double* x, double* z, const int* guard, Reduction red) {
   if (guard_off(guard)) return;
   double part = 0.0;

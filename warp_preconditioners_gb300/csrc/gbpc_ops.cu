@@ -29,7 +29,7 @@ namespace {
 
 // z = alpha * (d .* x) + beta * y   (d == nullptr: d = 1), optional dot(w, z).
 template <typename A>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 scale_axpby_kernel(int64_t n, const A* d, const A* x, const A* y, A* z, A alpha, A beta,
                    const int* guard, Reduction red) {
   if (guard_off(guard)) return;
@@ -47,7 +47,7 @@ scale_axpby_kernel(int64_t n, const A* d, const A* x, const A* y, A* z, A alpha,
 
 // Block diagonal apply: z_i = alpha * inv_i x_i + beta y_i (block_ilu.py:188-202).
 template <typename A, int B>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 block_diag_apply_kernel(int nrow, const A* __restrict__ inv, const A* x, const A* y, A* z, A alpha,
                         A beta, const int* guard, Reduction red) {
   if (guard_off(guard)) return;
@@ -142,7 +142,7 @@ __global__ void to_vector_dtype_kernel(int64_t n, const double* in, A* out) {
   if (i < n) out[i] = (A)in[i];
 }
 
-int elementwise_grid(int64_t n) { return std::min<int64_t>(grid_for(n, kThreads), kMaxCtas); }
+int elementwise_grid(int64_t n) { return std::min<int64_t>(grid_for(n, kThreads), kSms * kCtasPerSm); }
 
 Reduction make_reduction(const DotSpec* dot) {
   Reduction red{};

@@ -49,7 +49,11 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   double dot_part = 0.0;
-  for (int s = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); s < m.nslices; s += warps_total) {
+  // Warp w of CTA c starts at slice w * gridDim.x + c: the warps of one CTA
+  // work on slices far apart, so rows sorted by length inside windows do not
+  // leave one CTA with all the long rows (its warps wait for each other at
+  // the reduction barrier).
+  for (int s = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; s < m.nslices; s += warps_total) {
     const int row = s * kSlice + lane;
     const int64_t base = __ldg(m.slice_ptr + s);
     const int width = (int)((__ldg(m.slice_ptr + s + 1) - base) >> 5);
@@ -138,7 +142,7 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
 static int spmv_grid(int nslices, int minb) {
   const int warps_per_cta = kThreads / 32;
   int g = (nslices + warps_per_cta - 1) / warps_per_cta;
-  const int cap = 152 * minb;
+  const int cap = kSms * minb;
   if (g < 1) g = 1;
   if (g > cap) g = cap;
   return g;
@@ -153,7 +157,8 @@ static int spmv_flags(double alpha, double beta) {
 }
 
 // Product kernel variants for scalar rows: (entries loaded per chunk,
-// minimum resident CTAs per SM).  Blocked rows use one variant.
+// minimum resident 1024-thread CTAs per SM, i.e. a 32 or 64 register budget).
+// Blocked rows use one variant.
 constexpr int kNumVariants = 3;
 
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
@@ -169,22 +174,24 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
                            void* z, double alpha, double beta, int flags, const int* guard,
                            const EpiDev<A>& e, const Reduction& red, int nslices,
                            cudaStream_t st) {
-  if (B == 1) {
+  if constexpr (B == 1) {
     switch (variant) {
       case 1:
-        launch_one<B, V, A, EPI, DOT, 16, 4>(view, x, y, z, alpha, beta, flags, guard, e, red,
+        launch_one<B, V, A, EPI, DOT, 16, 1>(view, x, y, z, alpha, beta, flags, guard, e, red,
                                              nslices, st);
         return;
       case 2:
-        launch_one<B, V, A, EPI, DOT, 4, 8>(view, x, y, z, alpha, beta, flags, guard, e, red,
+        launch_one<B, V, A, EPI, DOT, 4, 2>(view, x, y, z, alpha, beta, flags, guard, e, red,
                                             nslices, st);
         return;
       default:
         break;
     }
   }
-  launch_one<B, V, A, EPI, DOT, Chunk<B>::value, 8>(view, x, y, z, alpha, beta, flags, guard, e,
-                                                    red, nslices, st);
+  // Blocked rows hold B*B values per entry: give them the 64-register budget.
+  constexpr int minb = (B == 1) ? kCtasPerSm : 1;
+  launch_one<B, V, A, EPI, DOT, Chunk<B>::value, minb>(view, x, y, z, alpha, beta, flags, guard, e,
+                                                       red, nslices, st);
 }
 
 template <int B, typename V, typename A, int EPI>
