@@ -71,7 +71,7 @@ _SIGNATURES = {
     "gbpc_op_destroy": [_vp],
     "gbpc_krylov": [_int, _vp, _vp, _vp, _vp, _dbl, _dbl, _int, _int, _vp, _vp, _vp, _i32p, _dp,
                     _dp, _vp],
-    "gbpc_solver_create": [_int, _vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
+    "gbpc_solver_create": [_int, _vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_solver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_solver_destroy": [_vp],
 }

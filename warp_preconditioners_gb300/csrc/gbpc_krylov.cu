@@ -120,6 +120,7 @@ struct Solver {
   Operator* M = nullptr;
   int64_t n = 0;
   bool use_graph = true;
+  int unroll = 8;  // iterations per pass of the device loop (measured: 1 -> 8 saves ~4 us/iteration)
   DevBuf r, z, p, Ap, Az, y, ks, zeros;
   ReduceBuf rb;
   // Cached graph for the last (b, x) pair.
@@ -284,7 +285,10 @@ struct Solver {
         rc = GBPC_ERR_CUDA;
         break;
       }
-      rc = record_iteration(x, cs);
+      // `unroll` guarded iterations per pass of the while-node: the loop
+      // condition is evaluated once per pass, and iterations after
+      // convergence inside a pass return immediately from every kernel.
+      for (int u = 0; u < unroll && !rc; ++u) rc = record_iteration(x, cs);
       e = cudaStreamEndCapture(cs, &g2);
       if (rc) break;
       if (e != cudaSuccess) {
@@ -372,8 +376,8 @@ struct gbpc_solver {
   Solver s;
 };
 
-extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_graph, void* stream,
-                                  gbpc_solver** out) {
+extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_graph, int unroll,
+                                  void* stream, gbpc_solver** out) {
   if (!out || !A || !A->impl || (method != GBPC_CG && method != GBPC_CR)) {
     gbpc_set_error("gbpc_solver_create: bad arguments");
     return GBPC_ERR_ARG;
@@ -396,6 +400,7 @@ extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_gr
   s.M = m;
   s.n = a->rows;
   s.use_graph = use_graph != 0;
+  if (unroll > 0) s.unroll = unroll > 64 ? 64 : unroll;
   const size_t bytes = sizeof(double) * std::max<int64_t>(s.n, 1);
   int rc = s.r.alloc(bytes);
   if (!rc) rc = s.z.alloc(bytes);
@@ -437,7 +442,7 @@ extern "C" int gbpc_krylov(int method, gbpc_op* A, gbpc_op* M, const double* b, 
                            double* rr_dev, double* atol_sq_dev, int32_t* nit_host,
                            double* rr_host, double* atol_sq_host, void* stream) {
   gbpc_solver* s = nullptr;
-  int rc = gbpc_solver_create(method, A, M, use_graph, stream, &s);
+  int rc = gbpc_solver_create(method, A, M, use_graph, 0, stream, &s);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   DevBuf outs;

@@ -98,13 +98,14 @@ def _handle(op: LinearOperator | None):
 class Solver:
     """Reusable CG / CR solver bound to (A, M); repeated runs replay one graph."""
 
-    def __init__(self, method: str, A, M=None, use_cuda_graph=True):
+    def __init__(self, method: str, A, M=None, use_cuda_graph=True, unroll=0):
         self.A = aslinearoperator(A)
         self.M = aslinearoperator(M)
         code = _lib.GBPC_CG if method == "cg" else _lib.GBPC_CR
         out = ctypes.c_void_p()
         _lib.call("gbpc_solver_create", code, _handle(self.A), _handle(self.M),
-                  int(bool(use_cuda_graph)), _lib.stream(self.A.device), ctypes.byref(out))
+                  int(bool(use_cuda_graph)), int(unroll), _lib.stream(self.A.device),
+                  ctypes.byref(out))
         self._h = out
         dev = self.A.device
         self.nit = torch.zeros(1, dtype=torch.int32, device=dev)
