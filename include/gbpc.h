@@ -235,11 +235,13 @@ int gbpc_krylov(int method, gbpc_op* A, gbpc_op* M, const double* b, double* x, 
 
 /* Reusable solver: owns the work vectors and a cached CUDA graph for the
  * last (b, x) pair, so repeated solves cost one graph launch each.
+ * `unroll` iterations (1..64, <= 0 selects the default 8) form one pass of
+ * the device loop; the stopping test still runs after every iteration.
  * gbpc_solver_run is stream-ordered and never synchronises; outputs as for
  * gbpc_krylov.  Same reference call sites as gbpc_krylov. */
 typedef struct gbpc_solver gbpc_solver;
-int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_graph, void* stream,
-                       gbpc_solver** out);
+int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_graph, int unroll,
+                       void* stream, gbpc_solver** out);
 int gbpc_solver_run(gbpc_solver* solver, const double* b, double* x, double tol, double atol,
                     int maxiter, int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
                     void* stream);
