@@ -302,16 +302,11 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    elapsed_ms = start.elapsed_time(end)
-    if dist:
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    value, elapsed_ms = replica_aggregate(start.elapsed_time(end), 4.0 * args.steps, dist, dev)
     ms_per_step = elapsed_ms / args.steps
     solve_ms = [r[0][0].elapsed_time(r[0][1]) for r in recs]
     setup_ms = [ms_per_step - s for s in solve_ms]
     iters = [[int(i.item()) for i in r[1]] for r in recs]
-    value = 4.0 * args.steps * world / (elapsed_ms / 1e3)
 
     # Accuracy of the last step against the assembled Q (float64, host).
     qh = prob["Q"]
@@ -380,6 +375,21 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def replica_aggregate(elapsed_ms, local_solves, dist, device):
+    """Whole-job throughput of independent replicas: every rank's solves over
+    the slowest rank's time (max over ranks)."""
+    import torch
+
+    if dist is None:
+        return local_solves / (elapsed_ms / 1e3), elapsed_ms
+    t = torch.tensor([elapsed_ms, float(local_solves)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    tot = t.clone()
+    dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+    return float(tot[1]) / (float(mx[0]) / 1e3), float(mx[0])
 
 
 def launch_count(iters):
@@ -487,12 +497,8 @@ def run_e2e(args, prob, dev, one_step, world, dist):
         step()
     e.record()
     torch.cuda.synchronize()
-    ms = s.elapsed_time(e)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    return {"value": 4.0 * args.steps * world / (ms / 1e3), "unit": "solves/s",
+    value, ms = replica_aggregate(s.elapsed_time(e), 4.0 * args.steps, dist, dev)
+    return {"value": value, "unit": "solves/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": ms / args.steps}
 
