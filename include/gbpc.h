@@ -233,6 +233,31 @@ int gbpc_krylov(int method, gbpc_op* A, gbpc_op* M, const double* b, double* x, 
                 double* atol_sq_dev, int32_t* nit_host, double* rr_host, double* atol_sq_host,
                 void* stream);
 
+/* FSAI application that allocates no device memory:
+ * z = alpha * G^T (G x) + beta * y from the CSR arrays of G and G^T
+ * (n x n, value_dtype F64 or F32; x, y, z float64 and device-resident).
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that cannot call cudaMalloc: hosts that hand the library a fixed pool of
+ * device memory and forbid further allocation, code paths that must stay
+ * free of allocation calls (device memory is exhausted or reserved by the
+ * host application, or allocation would synchronise or fail mid-pipeline).
+ * The intermediate G x lives in a static array inside libgbpc.so of
+ * gbpc_fsai_apply_noalloc_max_rows() = 524,288 float64 values (4 MiB), which
+ * every GPU that loads the library keeps until the process exits; larger n
+ * is rejected with GBPC_ERR_ARG.  The first call on each device looks up
+ * that array's device address (cudaGetSymbolAddress), so make the first call
+ * on a device before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU (different streams, no ordering) race and
+ * must be avoided.  x, y and z may alias; beta == 0 never reads y and
+ * alpha == 0 never reads x.  No cudaMalloc, cudaFree or allocating library
+ * routine is called. */
+int gbpc_fsai_apply_noalloc(int n, const int32_t* g_off, const int32_t* g_col, const void* g_val,
+                            const int32_t* gt_off, const int32_t* gt_col, const void* gt_val,
+                            int value_dtype, const double* x, const double* y, double* z,
+                            double alpha, double beta, void* stream);
+/* Row limit of gbpc_fsai_apply_noalloc. */
+int gbpc_fsai_apply_noalloc_max_rows(void);
+
 /* Reusable solver: owns the work vectors and a cached CUDA graph for the
  * last (b, x) pair, so repeated solves cost one graph launch each.
  * `unroll` iterations (1..64, <= 0 selects the default 8) form one pass of
