@@ -272,6 +272,51 @@ int gbpc_solver_run(gbpc_solver* solver, const double* b, double* x, double tol,
                     void* stream);
 int gbpc_solver_destroy(gbpc_solver* solver);
 
+/* ------------------------------------------------------------------------ */
+/* Many right-hand sides: batched operators, batched PCG, mixed-precision     */
+/* iterative refinement (no reference counterpart: the reference solves one   */
+/* right-hand side per call; these serve its repeated-solve call sites        */
+/* benchmarks/dragon.py:149-152 and visualization/solve_fields.py:121-124).   */
+/* ------------------------------------------------------------------------ */
+
+/* k <= 32 right-hand sides are stored row-major: row i of X is X[i*k..i*k+k).
+ * value_dtype is the storage of the matrix values (F64, F32 or BF16, converted
+ * on the device from in_dtype F64/F32 input); vector_dtype F64 or F32. */
+typedef struct gbpc_bop gbpc_bop;
+int gbpc_bop_sparse(int n, const int32_t* offsets, const int32_t* columns, const void* values,
+                    int in_dtype, int value_dtype, int vector_dtype, void* stream, gbpc_bop** out);
+int gbpc_bop_fsai(int n, const int32_t* g_off, const int32_t* g_col, const void* g_val,
+                  const int32_t* gt_off, const int32_t* gt_col, const void* gt_val, int in_dtype,
+                  int value_dtype, int vector_dtype, void* stream, gbpc_bop** out);
+/* Factored alpha M + L M^-1 L with every vertex free (L float64 input). */
+int gbpc_bop_sqlap(int n, const int32_t* offsets, const int32_t* columns, const void* values,
+                   int in_dtype, int value_dtype, int vector_dtype, const double* mass,
+                   double mass_weight, void* stream, gbpc_bop** out);
+/* Z = alpha * Op X + beta * Y for k right-hand sides (X must not alias Z). */
+int gbpc_bop_apply(gbpc_bop* op, int k, const void* X, const void* Y, void* Z, double alpha,
+                   double beta, void* stream);
+int gbpc_bop_destroy(gbpc_bop* op);
+
+/* Batched preconditioned CG: k independent recurrences over the same
+ * operator with per-right-hand-side scalars and stopping tests
+ * (r_j.r_j <= max(atol, tol |b_j|)^2 or maxiter), float64 dots, whole loop
+ * in one CUDA graph.  nit_dev[k], rr_dev[k] optional device outputs. */
+typedef struct gbpc_bsolver gbpc_bsolver;
+int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, void* stream, gbpc_bsolver** out);
+int gbpc_bsolver_run(gbpc_bsolver* solver, int k, const void* B, void* X, double tol,
+                     double atol, int maxiter, int32_t* nit_dev, double* rr_dev, void* stream);
+int gbpc_bsolver_destroy(gbpc_bsolver* solver);
+
+/* Mixed-precision iterative refinement: residual b - A64 x in float64 (A64
+ * a float64 batched operator), correction from `inner` (a batched solver,
+ * typically float32 operator and float32 / bfloat16 FSAI) to relative
+ * tolerance tol_inner, x += d in float64; right-hand side j stops once
+ * max|d_j| <= tol_outer * max|x_j|.  B, X float64 [n*k].  Synchronises once
+ * per outer step; outer_host[k] / inner_host[k] receive the counts. */
+int gbpc_refine(gbpc_bop* A64, gbpc_bsolver* inner, int k, const double* B, double* X,
+                double tol_outer, double tol_inner, int max_outer, int max_inner,
+                int32_t* outer_host, int32_t* inner_host, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,7 +12,7 @@ plus ``linear.cg`` / ``linear.cr`` / ``linear.preconditioner`` and the
 Vectors and matrices are torch CUDA tensors.
 """
 
-from . import linear, sparse
+from . import batched, linear, sparse
 from .biharmonic import BiharmonicSystem, RepeatedFSAI
 from .block_fsai import BlockFSAI, BsrBlockFSAI
 from .block_ilu import BlockILU0, BlockJacobi
@@ -41,6 +41,7 @@ __all__ = [
     "cg",
     "cr",
     "from_scipy",
+    "batched",
     "linear",
     "preconditioner",
     "sparse",

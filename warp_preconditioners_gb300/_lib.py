@@ -74,6 +74,17 @@ _SIGNATURES = {
     "gbpc_solver_create": [_int, _vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_solver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_solver_destroy": [_vp],
+    "gbpc_bop_sparse": [_int, _vp, _vp, _vp, _int, _int, _int, _vp, ctypes.POINTER(_vp)],
+    "gbpc_bop_fsai": [_int, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int, _vp,
+                      ctypes.POINTER(_vp)],
+    "gbpc_bop_sqlap": [_int, _vp, _vp, _vp, _int, _int, _int, _vp, _dbl, _vp,
+                       ctypes.POINTER(_vp)],
+    "gbpc_bop_apply": [_vp, _int, _vp, _vp, _vp, _dbl, _dbl, _vp],
+    "gbpc_bop_destroy": [_vp],
+    "gbpc_bsolver_create": [_vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
+    "gbpc_bsolver_run": [_vp, _int, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp],
+    "gbpc_bsolver_destroy": [_vp],
+    "gbpc_refine": [_vp, _vp, _int, _vp, _vp, _dbl, _dbl, _int, _int, _i32p, _i32p, _vp],
 }
 
 _lock = threading.Lock()
