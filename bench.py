@@ -61,6 +61,8 @@ def parse_args():
                    help="CG iterations per right-hand side in the CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mixed", action="store_true",
+                   help="skip the mixed-precision 32-RHS batched measurement")
     p.add_argument("--profile-iters", type=int, default=0,
                    help="profiling mode: one setup and one solve capped at this many "
                         "iterations, no timing (for ncu launch lists)")
@@ -360,6 +362,8 @@ def main():
     line["clocks"] = clk
     if not args.no_e2e:
         line["e2e"] = run_e2e(args, prob, dev, one_step, world, dist)
+    if not args.no_mixed:
+        line["mixed_batched"] = run_mixed_batched(args, prob, Q, K, mass, free, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline_sample(prob, args.width, args.step_size, args.method, args.cpu_iters,
                                  iters[-1])
@@ -390,6 +394,77 @@ def replica_aggregate(elapsed_ms, local_solves, dist, device):
     tot = t.clone()
     dist.all_reduce(tot, op=dist.ReduceOp.SUM)
     return float(tot[1]) / (float(mx[0]) / 1e3), float(mx[0])
+
+
+def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
+    """32 seeded U[-1,1] right-hand sides of the same system: mixed-precision
+    batched solve (float32 inner PCG on the factored operator with a bfloat16
+    FSAI factor, float64 refinement) against 32 sequential plain float64
+    solves, each including its setup."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, batched, linear
+
+    n = prob["n"]
+    b_np = np.stack([np.random.default_rng(s).uniform(-1, 1, n) for s in range(k)], 1)
+    B = torch.as_tensor(b_np, device=dev).contiguous()
+
+    def plain():
+        op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
+        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+        solver = linear.Solver("cg", op, pre)
+        xs = torch.zeros((k, n), dtype=torch.float64, device=dev)
+        b = torch.empty(n, dtype=torch.float64, device=dev)
+        its = []
+        for j in range(k):
+            b.copy_(B[:, j])
+            nit, _, _ = solver.run(b, xs[j], tol=args.rtol, maxiter=100000)
+            its.append(nit)
+        return xs, its
+
+    def mixed():
+        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+        ms = batched.MixedPrecisionSolver(K, mass, ALPHA, pre, torch.bfloat16)
+        X = torch.zeros_like(B)
+        outer, inner = ms.solve(B, X, tol_outer=1e-12, tol_inner=1e-3, max_outer=30)
+        return X, outer, inner
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    mixed()  # warm-up (module load, graph capture paths)
+    t_plain, (xs, its) = timed(plain)
+    t_mixed, (X, outer, inner) = timed(mixed)
+    qh = prob["Q"]
+    absq = abs(qh)
+    x_m = X.cpu().numpy()
+    x_p = xs.cpu().numpy().T
+    berr_m, berr_p, rel = [], [], []
+    for j in range(k):
+        den_m = absq @ np.abs(x_m[:, j]) + np.abs(b_np[:, j])
+        berr_m.append(float(np.max(np.abs(b_np[:, j] - qh @ x_m[:, j]) / den_m)))
+        den_p = absq @ np.abs(x_p[:, j]) + np.abs(b_np[:, j])
+        berr_p.append(float(np.max(np.abs(b_np[:, j] - qh @ x_p[:, j]) / den_p)))
+        rel.append(float(np.linalg.norm(x_m[:, j] - x_p[:, j]) / np.linalg.norm(x_p[:, j])))
+    return {
+        "workload": f"{k} seeded U[-1,1] RHS of the {args.side}^3 smoothing system; setup + solve",
+        "mixed_ms": t_mixed, "plain_fp64_sequential_ms": t_plain,
+        "mixed_solves_per_s": k / (t_mixed / 1e3), "plain_solves_per_s": k / (t_plain / 1e3),
+        "speedup": t_plain / t_mixed,
+        "mixed": "inner float32 PCG (float32 factored operator, bfloat16 FSAI w%d, float64 dots), "
+                 "float64 refinement; stop when max|dx| <= 1e-12 max|x|" % args.width,
+        "outer_iterations_max": int(max(outer)), "inner_iterations_max": int(max(inner)),
+        "plain_iterations_max": int(max(int(i.item()) for i in its)),
+        "backward_error_mixed_max": max(berr_m), "backward_error_plain_max": max(berr_p),
+        "rel_diff_vs_plain_fp64_max": max(rel),
+    }
 
 
 def launch_count(iters):
