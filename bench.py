@@ -422,11 +422,18 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             its.append(nit)
         return xs, its
 
+    def batch64():
+        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+        bs = batched.BatchedSolver(K, mass, ALPHA, pre)
+        X = torch.zeros_like(B)
+        nit, _ = bs.solve(B, X, tol=args.rtol, maxiter=100000)
+        return X, nit.clone()
+
     def mixed():
         pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
         ms = batched.MixedPrecisionSolver(K, mass, ALPHA, pre, torch.bfloat16)
         X = torch.zeros_like(B)
-        outer, inner = ms.solve(B, X, tol_outer=1e-12, tol_inner=1e-3, max_outer=30)
+        outer, inner = ms.solve(B, X, tol_outer=1e-12, tol_inner=1e-3, max_outer=8)
         return X, outer, inner
 
     def timed(fn):
@@ -439,31 +446,42 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1), out
 
-    mixed()  # warm-up (module load, graph capture paths)
+    batch64()  # warm-up (graph capture paths)
     t_plain, (xs, its) = timed(plain)
-    t_mixed, (X, outer, inner) = timed(mixed)
+    t_batch, (Xb, nitb) = timed(batch64)
+    t_mixed, (Xm, outer, inner) = timed(mixed)
     qh = prob["Q"]
     absq = abs(qh)
-    x_m = X.cpu().numpy()
     x_p = xs.cpu().numpy().T
-    berr_m, berr_p, rel = [], [], []
-    for j in range(k):
-        den_m = absq @ np.abs(x_m[:, j]) + np.abs(b_np[:, j])
-        berr_m.append(float(np.max(np.abs(b_np[:, j] - qh @ x_m[:, j]) / den_m)))
-        den_p = absq @ np.abs(x_p[:, j]) + np.abs(b_np[:, j])
-        berr_p.append(float(np.max(np.abs(b_np[:, j] - qh @ x_p[:, j]) / den_p)))
-        rel.append(float(np.linalg.norm(x_m[:, j] - x_p[:, j]) / np.linalg.norm(x_p[:, j])))
+
+    def quality(x):
+        berr, rel = [], []
+        for j in range(k):
+            den = absq @ np.abs(x[:, j]) + np.abs(b_np[:, j])
+            berr.append(float(np.max(np.abs(b_np[:, j] - qh @ x[:, j]) / den)))
+            rel.append(float(np.linalg.norm(x[:, j] - x_p[:, j]) / np.linalg.norm(x_p[:, j])))
+        return max(berr), max(rel)
+
+    berr_p, _ = quality(x_p)
+    berr_b, rel_b = quality(Xb.cpu().numpy())
+    berr_m, rel_m = quality(Xm.cpu().numpy())
     return {
         "workload": f"{k} seeded U[-1,1] RHS of the {args.side}^3 smoothing system; setup + solve",
-        "mixed_ms": t_mixed, "plain_fp64_sequential_ms": t_plain,
-        "mixed_solves_per_s": k / (t_mixed / 1e3), "plain_solves_per_s": k / (t_plain / 1e3),
-        "speedup": t_plain / t_mixed,
-        "mixed": "inner float32 PCG (float32 factored operator, bfloat16 FSAI w%d, float64 dots), "
-                 "float64 refinement; stop when max|dx| <= 1e-12 max|x|" % args.width,
-        "outer_iterations_max": int(max(outer)), "inner_iterations_max": int(max(inner)),
+        "plain_fp64_sequential_ms": t_plain, "plain_solves_per_s": k / (t_plain / 1e3),
         "plain_iterations_max": int(max(int(i.item()) for i in its)),
-        "backward_error_mixed_max": max(berr_m), "backward_error_plain_max": max(berr_p),
-        "rel_diff_vs_plain_fp64_max": max(rel),
+        "backward_error_plain_max": berr_p,
+        "batched_fp64": {
+            "solver": "one batched PCG for all %d RHS (float64 operator, vectors, FSAI w%d)"
+                      % (k, args.width),
+            "ms": t_batch, "solves_per_s": k / (t_batch / 1e3), "speedup": t_plain / t_batch,
+            "iterations_max": int(nitb.max().item()), "backward_error_max": berr_b,
+            "rel_diff_vs_plain_max": rel_b},
+        "float32_refinement": {
+            "solver": "inner float32 PCG (float32 factored operator, bfloat16 FSAI, float64 "
+                      "dots), float64 refinement, 8 outer steps max",
+            "ms": t_mixed, "speedup": t_plain / t_mixed, "outer_max": int(max(outer)),
+            "inner_max": int(max(inner)), "backward_error_max": berr_m,
+            "rel_diff_vs_plain_max": rel_m},
     }
 
 

@@ -139,6 +139,21 @@ def refine(A64: BatchedOperator, inner: BatchedCG, B, X, tol_outer=1e-12, tol_in
     return list(outer), list(inner_it)
 
 
+class BatchedSolver:
+    """k right-hand sides of the factored smoothing system in one float64
+    batched PCG (float64 operator and vectors; `factor_dtype` stores the FSAI
+    factor).  Matrix bytes are read once per iteration for the whole batch."""
+
+    def __init__(self, L: BsrMatrix, mass: torch.Tensor, mass_weight: float, pre: FSAI,
+                 factor_dtype=torch.float64, unroll=0):
+        self.A = batched_sqlap(L, mass, mass_weight, torch.float64, torch.float64)
+        self.M = batched_fsai(pre, factor_dtype, torch.float64)
+        self.cg = BatchedCG(self.A, self.M, unroll)
+
+    def solve(self, B, X, tol=1e-8, atol=0.0, maxiter=0):
+        return self.cg.run(B, X, tol, atol, maxiter)
+
+
 class MixedPrecisionSolver:
     """Float32 inner PCG with float64 refinement for the factored smoothing operator.
 
