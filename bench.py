@@ -61,6 +61,10 @@ def parse_args():
                    help="CG iterations per right-hand side in the CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--config", choices=["c2", "c3"], default="c2",
+                   help="c2: biharmonic smoothing (default); c3: K (x) C block coupling, "
+                        "every preconditioner under CG and CR")
+    p.add_argument("--c3-grid", type=int, default=64)
     p.add_argument("--no-mixed", action="store_true",
                    help="skip the mixed-precision 32-RHS batched measurement")
     p.add_argument("--profile-iters", type=int, default=0,
@@ -238,6 +242,10 @@ def main():
 
     from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, from_scipy, linear
 
+    if args.config == "c3":
+        if rank == 0:
+            print(json.dumps(run_c3(args, torch.device("cuda", local))), flush=True)
+        return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     dist = None
@@ -483,6 +491,77 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             "inner_max": int(max(inner)), "backward_error_max": berr_m,
             "rel_diff_vs_plain_max": rel_m},
     }
+
+
+def run_c3(args, dev, maxiter=20000):
+    """K (x) C block coupling: K = 7-point Dirichlet Laplacian on an n^3 grid,
+    C = R diag(1, 1, 1e-6) R^T with a seeded rotation, 3x3 blocks, float64;
+    every preconditioner of the reference's block benchmark
+    (benchmarks/block_challenge.py:249-261) under CG and CR to 1e-8, from
+    zero, on a U[-1,1] right-hand side.  Setup and solve are timed
+    separately with CUDA events (medians of 3)."""
+    import torch
+
+    from warp_preconditioners_gb300 import (BlockILU0, BlockJacobi, BsrBlockFSAI, FSAI, problems,
+                                            from_scipy, linear)
+
+    torch.cuda.set_device(dev)
+    bsr, c = problems.kron_coupling(args.c3_grid, 1e-6, seed=0)
+    bsr.sort_indices()
+    A = from_scipy(bsr.tocsr(), dev, torch.float64, (3, 3))
+    n = bsr.shape[0]
+    b_np = problems.uniform_rhs(n, 0)
+    b = torch.as_tensor(b_np, device=dev)
+    makers = {
+        "scalar_jacobi": lambda: linear.preconditioner(A, "diag"),
+        "block_jacobi": lambda: BlockJacobi(A, pivot_tolerance=1e-15),
+        "fsai_w8": lambda: FSAI(A, max_row_size=8, kap_tolerance=0.003,
+                                factor_dtype=torch.float32),
+        "block_fsai_2": lambda: BsrBlockFSAI(A, max_blocks=2, factor_dtype=torch.float32),
+        "block_fsai_4": lambda: BsrBlockFSAI(A, max_blocks=4, factor_dtype=torch.float32),
+        "block_ilu0_3_3": lambda: BlockILU0(A, factor_sweeps=3, solve_sweeps=3,
+                                            pivot_tolerance=1e-15),
+    }
+
+    def ev_time(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    rows = {}
+    for name, make in makers.items():
+        make()
+        setups = []
+        for _ in range(3):
+            t, pre = ev_time(make)
+            setups.append(t)
+        for method in ("cg", "cr"):
+            solver = linear.Solver(method, A, pre)
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            solver.run(b, x, tol=args.rtol, maxiter=maxiter)
+            times = []
+            for _ in range(3):
+                x.zero_()
+                t, (nit, rr, at) = ev_time(lambda: solver.run(b, x, tol=args.rtol,
+                                                              maxiter=maxiter))
+                times.append(t)
+            sol = x.cpu().numpy()
+            rel = float(np.linalg.norm(b_np - bsr @ sol) / np.linalg.norm(b_np))
+            it = int(nit.item())
+            rows[f"{name}/{method}"] = {
+                "setup_ms": statistics.median(setups), "solve_ms": statistics.median(times),
+                "total_ms": statistics.median(setups) + statistics.median(times),
+                "iterations": it, "converged": bool(rr.item() <= at.item()),
+                "true_relres": rel}
+    return {"config": {"workload": f"K (x) C, {args.c3_grid}^3 7-point Laplacian, C = R diag(1,1,"
+                                   f"1e-6) R^T, 3x3 BSR float64, {n} unknowns, CG/CR to "
+                                   f"{args.rtol:g} (max {maxiter} iterations), U[-1,1] RHS"},
+            "metric": "setup+solve ms per preconditioner and solver", "results": rows}
 
 
 def launch_count(iters):
