@@ -27,6 +27,7 @@ all ranks' solves over the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import math
 import os
@@ -61,10 +62,19 @@ def parse_args():
                    help="CG iterations per right-hand side in the CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--config", choices=["c2", "c3"], default="c2",
+    p.add_argument("--config", choices=["c2", "c3", "c5"], default="c2",
                    help="c2: biharmonic smoothing (default); c3: K (x) C block coupling, "
-                        "every preconditioner under CG and CR")
+                        "every preconditioner under CG and CR; c5: serving stream")
     p.add_argument("--c3-grid", type=int, default=64)
+    p.add_argument("--c5-requests", type=int, default=200,
+                   help="requests replayed from the seed-0 stream (its first N of 2,000)")
+    p.add_argument("--c5-rate", type=float, default=4.0, help="Poisson arrivals per second")
+    p.add_argument("--c5-slots", type=int, default=16)
+    p.add_argument("--c5-budget-gb", type=float, default=120.0)
+    p.add_argument("--c5-nmin", type=float, default=5e3)
+    p.add_argument("--c5-nmax", type=float, default=5e5)
+    p.add_argument("--c5-no-sequential", action="store_true",
+                   help="skip the one-at-a-time float64 arm")
     p.add_argument("--no-mixed", action="store_true",
                    help="skip the mixed-precision 32-RHS batched measurement")
     p.add_argument("--profile-iters", type=int, default=0,
@@ -245,6 +255,10 @@ def main():
     if args.config == "c3":
         if rank == 0:
             print(json.dumps(run_c3(args, torch.device("cuda", local))), flush=True)
+        return
+    if args.config == "c5":
+        if rank == 0:
+            print(json.dumps(run_c5(args, torch.device("cuda", local))), flush=True)
         return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -562,6 +576,88 @@ def run_c3(args, dev, maxiter=20000):
                                    f"1e-6) R^T, 3x3 BSR float64, {n} unknowns, CG/CR to "
                                    f"{args.rtol:g} (max {maxiter} iterations), U[-1,1] RHS"},
             "metric": "setup+solve ms per preconditioner and solver", "results": rows}
+
+
+def run_c5(args, dev):
+    """Serving stream: the first --c5-requests requests of the seed-0 stream of
+    2,000 (Laplacian or tet-cube biharmonic, n log-uniform on [5e3, 5e5],
+    1-8 U[-1,1] right-hand sides, Poisson arrivals at --c5-rate per second),
+    CG + FSAI w8 to 1e-8 relative residual, systems resident under the HBM
+    budget.  Served with continuous batching into slots, then replayed on the
+    plain one-at-a-time float64 path; latency is from the scheduled arrival
+    to x back in host memory.  Each arm also replays the same requests all
+    arriving at once ("burst"): its solves/s is the arm's capacity."""
+    import torch
+
+    from warp_preconditioners_gb300 import serve
+
+    torch.cuda.set_device(dev)
+    full = serve.request_stream(2000, args.c5_rate, seed=0, n_min=args.c5_nmin,
+                                n_max=args.c5_nmax)
+    stream = full[:args.c5_requests]
+    keys = list(dict.fromkeys(r.key for r in stream))
+    cat = serve.Catalog()
+    t0 = time.perf_counter()
+    cat.prebuild(keys, threads=min(16, os.cpu_count() or 4))
+    assembly_s = time.perf_counter() - t0
+
+    budget = args.c5_budget_gb * 1e9
+    ex = serve.GpuExecutor(cat, slots=args.c5_slots, tol=args.rtol, device=dev)
+    srv = serve.Server(ex, budget_bytes=budget)
+    t0 = time.perf_counter()
+    srv.prepare(keys)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    burst = [serve.Request(r.rid, r.kind, r.side, r.k, 0.0, r.seed) for r in stream]
+    keep = lambda r: r.rid % 10 == 0
+    with ClockSampler(dev.index or 0) as clk:
+        served = srv.run(stream, keep=keep)
+        served_burst = srv.run(burst, keep=lambda r: False)
+    clocks = clk.summary()
+    out = {"served": serve.summarize(served), "served_burst": serve.summarize(served_burst)}
+
+    # Every tenth request, on the host (untimed): relative residual
+    # |b - A x| / |b| and componentwise backward error
+    # max_i |b - A x|_i / (|A| |x| + |b|)_i.  For the alpha = 1e-4 biharmonic
+    # systems the first is dominated by cancellation in forming b - A x
+    # (|A| |x| >> |b|); the second is the accuracy measure.
+    worst_rel = worst_berr = 0.0
+    for req, r in zip(stream, served):
+        if r.ok and r.x is not None:
+            h = cat.get(req.key)
+            A = h.A if h.kind == "laplacian" else h.P
+            b, x = serve.request_rhs(req).numpy(), r.x.numpy()
+            res = b - A @ x
+            worst_rel = max(worst_rel, float((np.linalg.norm(res, axis=0)
+                                              / np.linalg.norm(b, axis=0)).max()))
+            den = abs(A) @ np.abs(x) + np.abs(b)
+            worst_berr = max(worst_berr, float((np.abs(res) / den).max()))
+    out["served"]["relres_max_sampled"] = worst_rel
+    out["served"]["backward_error_max_sampled"] = worst_berr
+
+    if not args.c5_no_sequential:
+        seq_ex = serve.GpuExecutor(cat, sequential=True, tol=args.rtol, device=dev)
+        seq = serve.Server(seq_ex, budget_bytes=budget)
+        seq.resident, seq.used, seq.peak = srv.resident, srv.used, srv.peak  # same systems
+        out["sequential"] = serve.summarize(seq.run(stream, keep=lambda r: False))
+        out["sequential_burst"] = serve.summarize(seq.run(burst, keep=lambda r: False))
+        s, q = out["served"], out["sequential"]
+        sb, qb = out["served_burst"], out["sequential_burst"]
+        out["speedup"] = {"capacity_solves_per_s": sb["solves_per_s"] / qb["solves_per_s"],
+                          "p50": q["p50_ms"] / s["p50_ms"], "p99": q["p99_ms"] / s["p99_ms"]}
+    kinds = collections.Counter(r.kind for r in stream)
+    return {
+        "metric": "serving p50/p99 latency (ms) and solves/s at 1e-8 relative residual",
+        "unit": "ms, solves/s", "higher_is_better": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"serving stream: first {len(stream)} of 2,000 seeded requests "
+                               f"(seed 0), Poisson {args.c5_rate:g}/s, n log-uniform "
+                               f"[{args.c5_nmin:g}, {args.c5_nmax:g}], 1-8 U[-1,1] RHS, "
+                               f"{dict(kinds)}; CG + FSAI w8 to {args.rtol:g}",
+                   "slots": ex.slots, "budget_gb": args.c5_budget_gb,
+                   "systems": len(keys)},
+        "host_assembly_s": assembly_s, "device_setup_s": setup_s,
+        "resident_gb": srv.used / 1e9, "resident_peak_gb": srv.peak / 1e9,
+        "server_stats": srv.stats, "clocks": clocks, **out}
 
 
 def launch_count(iters):

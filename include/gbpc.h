@@ -28,6 +28,7 @@
 #ifndef GBPC_H
 #define GBPC_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -58,6 +59,10 @@ enum gbpc_method { GBPC_CG = 0, GBPC_CR = 1 };
 const char* gbpc_last_error(void);
 /* ABI version, currently 1. */
 int gbpc_version(void);
+/* Device bytes held by every live allocation of the library (operators,
+ * solvers and their scratch; the fixed array of gbpc_fsai_apply_noalloc is
+ * not counted).  No reference counterpart: serving admission control. */
+int gbpc_device_bytes(size_t* live_host);
 
 /* ------------------------------------------------------------------------ */
 /* FSAI setup stages                                                         */
@@ -211,6 +216,9 @@ int gbpc_op_apply(gbpc_op* op, const void* x, const void* y, void* z, double alp
 /* Scalar length of the operator's vectors. */
 int gbpc_op_rows(const gbpc_op* op, int64_t* rows_host);
 
+/* Device bytes the operator holds (matrices, factors, scratch). */
+int gbpc_op_device_bytes(const gbpc_op* op, size_t* bytes_host);
+
 /* Release an operator and its device memory (synchronises the device). */
 int gbpc_op_destroy(gbpc_op* op);
 
@@ -271,6 +279,8 @@ int gbpc_solver_run(gbpc_solver* solver, const double* b, double* x, double tol,
                     int maxiter, int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
                     void* stream);
 int gbpc_solver_destroy(gbpc_solver* solver);
+/* Device bytes of the solver's Krylov state (work vectors, scalars). */
+int gbpc_solver_device_bytes(const gbpc_solver* solver, size_t* bytes_host);
 
 /* ------------------------------------------------------------------------ */
 /* Many right-hand sides: batched operators, batched PCG, mixed-precision     */
@@ -285,16 +295,18 @@ int gbpc_solver_destroy(gbpc_solver* solver);
 typedef struct gbpc_bop gbpc_bop;
 int gbpc_bop_sparse(int n, const int32_t* offsets, const int32_t* columns, const void* values,
                     int in_dtype, int value_dtype, int vector_dtype, void* stream, gbpc_bop** out);
+/* max_rhs (1..32) sizes the operator's scratch: applies take k <= max_rhs. */
 int gbpc_bop_fsai(int n, const int32_t* g_off, const int32_t* g_col, const void* g_val,
                   const int32_t* gt_off, const int32_t* gt_col, const void* gt_val, int in_dtype,
-                  int value_dtype, int vector_dtype, void* stream, gbpc_bop** out);
+                  int value_dtype, int vector_dtype, int max_rhs, void* stream, gbpc_bop** out);
 /* Factored alpha M + L M^-1 L with every vertex free (L float64 input). */
 int gbpc_bop_sqlap(int n, const int32_t* offsets, const int32_t* columns, const void* values,
                    int in_dtype, int value_dtype, int vector_dtype, const double* mass,
-                   double mass_weight, void* stream, gbpc_bop** out);
+                   double mass_weight, int max_rhs, void* stream, gbpc_bop** out);
 /* Z = alpha * Op X + beta * Y for k right-hand sides (X must not alias Z). */
 int gbpc_bop_apply(gbpc_bop* op, int k, const void* X, const void* Y, void* Z, double alpha,
                    double beta, void* stream);
+int gbpc_bop_device_bytes(const gbpc_bop* op, size_t* bytes_host);
 int gbpc_bop_destroy(gbpc_bop* op);
 
 /* Batched preconditioned CG: k independent recurrences over the same
@@ -302,9 +314,11 @@ int gbpc_bop_destroy(gbpc_bop* op);
  * (r_j.r_j <= max(atol, tol |b_j|)^2 or maxiter), float64 dots, whole loop
  * in one CUDA graph.  nit_dev[k], rr_dev[k] optional device outputs. */
 typedef struct gbpc_bsolver gbpc_bsolver;
-int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, void* stream, gbpc_bsolver** out);
+int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, int max_rhs, void* stream,
+                        gbpc_bsolver** out);
 int gbpc_bsolver_run(gbpc_bsolver* solver, int k, const void* B, void* X, double tol,
                      double atol, int maxiter, int32_t* nit_dev, double* rr_dev, void* stream);
+int gbpc_bsolver_device_bytes(const gbpc_bsolver* solver, size_t* bytes_host);
 int gbpc_bsolver_destroy(gbpc_bsolver* solver);
 
 /* Mixed-precision iterative refinement: residual b - A64 x in float64 (A64

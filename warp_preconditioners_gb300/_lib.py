@@ -44,10 +44,12 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _vp = ctypes.c_void_p
 _int = ctypes.c_int
 _dbl = ctypes.c_double
+_szp = ctypes.POINTER(ctypes.c_size_t)
 
 # name -> argtypes (all functions return int status)
 _SIGNATURES = {
     "gbpc_version": [],
+    "gbpc_device_bytes": [_szp],
     "gbpc_fsai_setup": [_int, _vp, _vp, _vp, _int, _int, _int, _dbl, _dbl, _vp, _vp, _vp, _vp,
                         _i32p, _vp],
     "gbpc_fsai_pack": [_int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _i64p, _vp],
@@ -68,21 +70,25 @@ _SIGNATURES = {
     "gbpc_bsr_transpose": [_int, _int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp],
     "gbpc_op_apply": [_vp, _vp, _vp, _vp, _dbl, _dbl, _vp],
     "gbpc_op_rows": [_vp, _i64p],
+    "gbpc_op_device_bytes": [_vp, _szp],
     "gbpc_op_destroy": [_vp],
     "gbpc_krylov": [_int, _vp, _vp, _vp, _vp, _dbl, _dbl, _int, _int, _vp, _vp, _vp, _i32p, _dp,
                     _dp, _vp],
     "gbpc_solver_create": [_int, _vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_solver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_solver_destroy": [_vp],
+    "gbpc_solver_device_bytes": [_vp, _szp],
     "gbpc_bop_sparse": [_int, _vp, _vp, _vp, _int, _int, _int, _vp, ctypes.POINTER(_vp)],
-    "gbpc_bop_fsai": [_int, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int, _vp,
+    "gbpc_bop_fsai": [_int, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int, _int, _vp,
                       ctypes.POINTER(_vp)],
-    "gbpc_bop_sqlap": [_int, _vp, _vp, _vp, _int, _int, _int, _vp, _dbl, _vp,
+    "gbpc_bop_sqlap": [_int, _vp, _vp, _vp, _int, _int, _int, _vp, _dbl, _int, _vp,
                        ctypes.POINTER(_vp)],
     "gbpc_bop_apply": [_vp, _int, _vp, _vp, _vp, _dbl, _dbl, _vp],
+    "gbpc_bop_device_bytes": [_vp, _szp],
     "gbpc_bop_destroy": [_vp],
-    "gbpc_bsolver_create": [_vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
+    "gbpc_bsolver_create": [_vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_bsolver_run": [_vp, _int, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp],
+    "gbpc_bsolver_device_bytes": [_vp, _szp],
     "gbpc_bsolver_destroy": [_vp],
     "gbpc_refine": [_vp, _vp, _int, _vp, _vp, _dbl, _dbl, _int, _int, _i32p, _i32p, _vp],
 }
@@ -162,6 +168,20 @@ def stream(device=None):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
+def object_bytes(getter: str, handle) -> int:
+    """Device bytes held by a library object (`getter` is its *_device_bytes)."""
+    out = ctypes.c_size_t()
+    call(getter, handle, ctypes.byref(out))
+    return int(out.value)
+
+
+def live_device_bytes() -> int:
+    """Device bytes held by every live allocation of the library."""
+    out = ctypes.c_size_t()
+    call("gbpc_device_bytes", ctypes.byref(out))
+    return int(out.value)
+
+
 class OpHandle:
     """Owns a gbpc_op*."""
 
@@ -177,6 +197,10 @@ class OpHandle:
             except Exception:
                 pass
             self.handle = None
+
+    @property
+    def device_bytes(self) -> int:
+        return object_bytes("gbpc_op_device_bytes", self.handle)
 
     def apply(self, x, y, z, alpha, beta, device=None):
         check(load().gbpc_op_apply(self.handle, ptr(x), ptr(y) if y is not None else None, ptr(z),

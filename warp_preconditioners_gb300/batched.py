@@ -1,9 +1,9 @@
 """Many right-hand sides of one system: batched operators, batched PCG and
 mixed-precision iterative refinement.
 
-Vectors are ``[n, k]`` row-major tensors with ``k <= 32``.  One warp per
-matrix row serves all k right-hand sides, so matrix bytes are read once per
-iteration for the whole batch.  ``MixedPrecisionSolver`` runs the inner PCG in
+Vectors are ``[n, k]`` row-major tensors with ``k <= 32``.  A group of
+k-rounded-up-to-a-power-of-two lanes serves all k right-hand sides of a
+matrix row, so matrix bytes are read once per iteration for the whole batch.  ``MixedPrecisionSolver`` runs the inner PCG in
 float32 (float32 operator, float32 or bfloat16 FSAI factor, float64 dots) and
 corrects in float64 with the float64 factored operator: iterative refinement
 recovers float64 accuracy (componentwise backward error ~1e-15 on the
@@ -26,11 +26,16 @@ MAX_RHS = 32
 class BatchedOperator:
     """Z = alpha * Op X + beta * Y for [n, k] blocks of vectors."""
 
-    def __init__(self, handle, rows, vector_dtype, device):
+    def __init__(self, handle, rows, vector_dtype, device, max_rhs=MAX_RHS):
         self._h = handle
         self.rows = rows
         self.dtype = vector_dtype
         self.device = device
+        self.max_rhs = max_rhs
+
+    @property
+    def device_bytes(self) -> int:
+        return _lib.object_bytes("gbpc_bop_device_bytes", self._h)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -41,24 +46,30 @@ class BatchedOperator:
                 pass
 
     def apply(self, X, Y, Z, alpha=1.0, beta=0.0):
-        k = _check_block(X, self.rows, self.dtype)
+        k = _check_block(X, self.rows, self.dtype, self.max_rhs)
         _lib.call("gbpc_bop_apply", self._h, k, _lib.ptr(X), _lib.ptr(Y) if Y is not None else None,
                   _lib.ptr(Z), float(alpha), float(beta), _lib.stream(self.device))
         return Z
 
 
-def _check_block(X, rows, dtype):
-    if X.dim() != 2 or X.shape[0] != rows or not 1 <= X.shape[1] <= MAX_RHS:
-        raise ValueError(f"expected an [{rows}, k] block with 1 <= k <= {MAX_RHS}")
+def _check_block(X, rows, dtype, max_rhs=MAX_RHS):
+    if X.dim() != 2 or X.shape[0] != rows or not 1 <= X.shape[1] <= max_rhs:
+        raise ValueError(f"expected an [{rows}, k] block with 1 <= k <= {max_rhs}")
     if X.dtype != dtype:
         raise TypeError(f"expected {dtype} vectors, got {X.dtype}")
     return int(X.shape[1])
 
 
-def _new(name, *args, rows, vdt, device):
+def _new(name, *args, rows, vdt, device, max_rhs=MAX_RHS):
     out = ctypes.c_void_p()
     _lib.call(name, *args, ctypes.byref(out))
-    return BatchedOperator(out, rows, vdt, device)
+    return BatchedOperator(out, rows, vdt, device, max_rhs)
+
+
+def _max_rhs(max_rhs):
+    if isinstance(max_rhs, bool) or not isinstance(max_rhs, int) or not 1 <= max_rhs <= MAX_RHS:
+        raise ValueError(f"max_rhs must be an integer in [1, {MAX_RHS}]")
+    return max_rhs
 
 
 def batched_sparse(A: BsrMatrix, value_dtype=None, vector_dtype=None) -> BatchedOperator:
@@ -72,7 +83,8 @@ def batched_sparse(A: BsrMatrix, value_dtype=None, vector_dtype=None) -> Batched
                 rows=A.nrow, vdt=vector_dtype, device=A.device)
 
 
-def batched_fsai(pre: FSAI, value_dtype=None, vector_dtype=None) -> BatchedOperator:
+def batched_fsai(pre: FSAI, value_dtype=None, vector_dtype=None,
+                 max_rhs=MAX_RHS) -> BatchedOperator:
     g, gt = pre.G, pre.GT
     if g.scalar_type == torch.bfloat16:
         raise ValueError("build the FSAI in float32 or float64; narrow with value_dtype")
@@ -81,12 +93,12 @@ def batched_fsai(pre: FSAI, value_dtype=None, vector_dtype=None) -> BatchedOpera
     return _new("gbpc_bop_fsai", g.nrow, _lib.ptr(g.offsets), _lib.ptr(g.columns),
                 _lib.ptr(g.values), _lib.ptr(gt.offsets), _lib.ptr(gt.columns),
                 _lib.ptr(gt.values), _lib.dtype_code(g.scalar_type), _lib.dtype_code(value_dtype),
-                _lib.dtype_code(vector_dtype), _lib.stream(g.device),
-                rows=g.nrow, vdt=vector_dtype, device=g.device)
+                _lib.dtype_code(vector_dtype), _max_rhs(max_rhs), _lib.stream(g.device),
+                rows=g.nrow, vdt=vector_dtype, device=g.device, max_rhs=max_rhs)
 
 
 def batched_sqlap(L: BsrMatrix, mass: torch.Tensor, mass_weight: float, value_dtype=torch.float64,
-                  vector_dtype=None) -> BatchedOperator:
+                  vector_dtype=None, max_rhs=MAX_RHS) -> BatchedOperator:
     """Factored ``mass_weight * M + L M^-1 L`` with every vertex free."""
     if L.scalar_type != torch.float64 or mass.dtype != torch.float64:
         raise TypeError("pass float64 L and mass; value_dtype selects the stored precision")
@@ -94,17 +106,19 @@ def batched_sqlap(L: BsrMatrix, mass: torch.Tensor, mass_weight: float, value_dt
     return _new("gbpc_bop_sqlap", L.nrow, _lib.ptr(L.offsets), _lib.ptr(L.columns),
                 _lib.ptr(L.values), _lib.GBPC_F64, _lib.dtype_code(value_dtype),
                 _lib.dtype_code(vector_dtype), _lib.ptr(mass.contiguous()), float(mass_weight),
-                _lib.stream(L.device), rows=L.nrow, vdt=vector_dtype, device=L.device)
+                _max_rhs(max_rhs), _lib.stream(L.device), rows=L.nrow, vdt=vector_dtype,
+                device=L.device, max_rhs=max_rhs)
 
 
 class BatchedCG:
     """k independent PCG recurrences on one operator, per-RHS stopping."""
 
-    def __init__(self, A: BatchedOperator, M: BatchedOperator, unroll=0):
+    def __init__(self, A: BatchedOperator, M: BatchedOperator, unroll=0, max_rhs=None):
         self.A, self.M = A, M
+        self.max_rhs = _max_rhs(max_rhs if max_rhs is not None else min(A.max_rhs, M.max_rhs))
         out = ctypes.c_void_p()
-        _lib.call("gbpc_bsolver_create", A._h, M._h, int(unroll), _lib.stream(A.device),
-                  ctypes.byref(out))
+        _lib.call("gbpc_bsolver_create", A._h, M._h, int(unroll), self.max_rhs,
+                  _lib.stream(A.device), ctypes.byref(out))
         self._h = out
         self.nit = torch.zeros(MAX_RHS, dtype=torch.int32, device=A.device)
         self.rr = torch.zeros(MAX_RHS, dtype=torch.float64, device=A.device)
@@ -117,9 +131,13 @@ class BatchedCG:
             except Exception:
                 pass
 
+    @property
+    def device_bytes(self) -> int:
+        return _lib.object_bytes("gbpc_bsolver_device_bytes", self._h)
+
     def run(self, B, X, tol=1e-8, atol=0.0, maxiter=0):
-        k = _check_block(B, self.A.rows, self.A.dtype)
-        _check_block(X, self.A.rows, self.A.dtype)
+        k = _check_block(B, self.A.rows, self.A.dtype, self.max_rhs)
+        _check_block(X, self.A.rows, self.A.dtype, self.max_rhs)
         _lib.call("gbpc_bsolver_run", self._h, k, _lib.ptr(B), _lib.ptr(X), float(tol),
                   float(atol), int(maxiter), _lib.ptr(self.nit), _lib.ptr(self.rr),
                   _lib.stream(self.A.device))

@@ -2,22 +2,26 @@
 // refinement.
 //
 // Vectors hold k <= 32 right-hand sides per row, row-major (row i of X is
-// X[i*k .. i*k+k)).  A product is one warp per matrix row with lane j working
-// on right-hand side j: the warp reads each stored entry once (a coalesced
-// load of up to 32 entries, then shuffles) and gathers the k values of x's
-// row in one coalesced access, so matrix bytes are shared by all right-hand
-// sides.  In float32 this turns the FP64-bound single-vector product into an
-// L2/HBM-bound one.
+// X[i*k .. i*k+k)).  A warp works on 32/KP consecutive rows at once, each on
+// a group of KP lanes (KP = k rounded up to a power of two) with lane j of the
+// group on right-hand side j.  A group reads each stored entry of its row once
+// (a coalesced load of up to KP entries, then shuffles inside the group) and
+// gathers the k values of x's row in one access, so matrix bytes are shared by
+// all right-hand sides, and the FP64 instructions issued per right-hand side
+// are those of k/KP single-vector products (the warp-wide FP64 issue rate does
+// not depend on how many lanes are active).
 //
-// Dots are accumulated in float64 per right-hand side, reduced per CTA
-// through shared memory and combined in index order by the last CTA to
-// finish (deterministic).  Every right-hand side has its own CG scalars and
-// stopping test; finished ones are masked out while the rest continue.
+// Dots are accumulated in float64 per right-hand side, folded across the row
+// groups of a warp, reduced per CTA through shared memory and combined in
+// index order by the last CTA to finish (deterministic for a given k).  Every
+// right-hand side has its own CG scalars and stopping test; finished ones are
+// masked out while the rest continue.
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <vector>
 
 #include "gbpc_common.cuh"
@@ -71,6 +75,23 @@ template <> __device__ __forceinline__ double cvt<double, double>(double v) { re
 template <> __device__ __forceinline__ double cvt<double, float>(float v) { return (double)v; }
 template <> __device__ __forceinline__ double cvt<double, __nv_bfloat16>(__nv_bfloat16 v) {
   return (double)__bfloat162float(v);
+}
+
+// Lanes per row group for k right-hand sides (k rounded up to a power of 2).
+static inline int kp_for(int k) {
+  int kp = 1;
+  while (kp < k) kp <<= 1;
+  return kp;
+}
+
+// Per right-hand-side total over the row groups of a warp: lanes with the
+// same index inside their group are summed (a fixed butterfly); lane j < KP
+// returns the total for right-hand side j, the other lanes 0.
+template <int KP>
+__device__ __forceinline__ double b_fold(double v) {
+#pragma unroll
+  for (int o = KP; o < 32; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return (threadIdx.x & 31) < KP ? v : 0.0;
 }
 
 __device__ __forceinline__ void b_set_active(BatchScalars* bs, int j, bool valid) {
@@ -164,41 +185,60 @@ __device__ __forceinline__ void b_reduce(const BRed& red, double v) {
 
 enum BEpi : int { BE_AXPBY = 0, BE_SQLAP_BWD = 1 };
 
-// Z = alpha * A X + beta * Y (or the factored backward epilogue), warp per
-// row, lane = right-hand side.  Row-scaled forward products pass the scaled
-// matrix.  `flags` as in the single-vector product.
-template <typename V, typename T, int EPI, bool DOT>
-__global__ void __launch_bounds__(kBThreads)
+// Z = alpha * A X + beta * Y (or the factored backward epilogue).  A warp
+// handles 32/KP consecutive rows, one per group of KP lanes; lane j of a
+// group works on right-hand side j.  Row-scaled forward products pass the
+// scaled matrix.  Each row sums its entries in storage order, whatever KP.
+template <typename V, typename T, int EPI, bool DOT, int KP>
+__global__ void __launch_bounds__(kBThreads, 2)
 bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __restrict__ col,
              const V* __restrict__ val, const T* X, const T* Y, T* Z, double alpha, double beta,
              int alpha_zero, int alpha_one, int beta_zero, const T* wm, const T* X2,
              const int* guard, BRed red) {
   if (guard_off(guard)) return;
+  constexpr int GR = 32 / KP;
   const int lane = threadIdx.x & 31;
-  const int warps_total = gridDim.x * kBWarps;
-  const bool on = lane < k;
+  const int grp = lane / KP, j = lane % KP;
+  const int64_t warps_total = (int64_t)gridDim.x * kBWarps;
+  const bool on = j < k;
   double dot = 0.0;
-  for (int row = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; row < nrow; row += warps_total) {
+  for (int64_t wb = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; wb * GR < nrow;
+       wb += warps_total) {
+    const int row = (int)(wb * GR) + grp;
+    const bool live = row < nrow;
     T acc = T(0);
     if (!alpha_zero) {
-      const int e0 = __ldg(off + row), e1 = __ldg(off + row + 1);
-      for (int base = e0; base < e1; base += 32) {
-        const int cnt = min(32, e1 - base);
-        int c_l = 0;
-        T v_l = T(0);
-        if (lane < cnt) {
-          c_l = __ldg(col + base + lane);
-          v_l = cvt<T, V>(__ldg(val + base + lane));
-        }
-        for (int e = 0; e < cnt; ++e) {
-          const int c = __shfl_sync(0xffffffffu, c_l, e);
-          const T v = __shfl_sync(0xffffffffu, v_l, e);
-          if (on) acc = fma_bt<T>(v, X[(int64_t)c * k + lane], acc);
+      int e0 = 0, len = 0;
+      if (live) {
+        e0 = __ldg(off + row);
+        len = __ldg(off + row + 1) - e0;
+      }
+      int maxlen = len;
+#pragma unroll
+      for (int o = KP; o < 32; o <<= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+      for (int base = 0; base < maxlen; base += KP) {
+        if constexpr (KP == 1) {
+          if (base < len)
+            acc = fma_bt<T>(cvt<T, V>(__ldg(val + e0 + base)),
+                            X[(int64_t)__ldg(col + e0 + base) * k], acc);
+        } else {
+          int c_l = 0;
+          T v_l = T(0);
+          if (base + j < len) {
+            c_l = __ldg(col + e0 + base + j);
+            v_l = cvt<T, V>(__ldg(val + e0 + base + j));
+          }
+          const int cnt = min(KP, maxlen - base);
+          for (int e = 0; e < cnt; ++e) {
+            const int c = __shfl_sync(0xffffffffu, c_l, e, KP);
+            const T v = __shfl_sync(0xffffffffu, v_l, e, KP);
+            if (on && base + e < len) acc = fma_bt<T>(v, X[(int64_t)c * k + j], acc);
+          }
         }
       }
     }
-    if (on) {
-      const int64_t idx = (int64_t)row * k + lane;
+    if (on && live) {
+      const int64_t idx = (int64_t)row * k + j;
       T out;
       if (EPI == BE_SQLAP_BWD) {
         out = T(0);
@@ -214,37 +254,49 @@ bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __
       if (DOT) dot = fma((double)out, (double)((const T*)red.w)[idx], dot);
     }
   }
-  if (DOT) b_reduce(red, dot);
+  if (DOT) b_reduce(red, b_fold<KP>(dot));
 }
 
 // ---------------------------------------------------------------------------
 // Batched CG kernels (vectors T, scalars float64).
 
-template <typename T>
+// Rows of the elementwise kernels follow the same groups as the product.
+#define B_ROWS(KP)                                                                     \
+  constexpr int GR = 32 / (KP);                                                       \
+  const int lane = threadIdx.x & 31;                                                  \
+  const int grp = lane / (KP), j = lane % (KP);                                       \
+  const int64_t warps_total = (int64_t)gridDim.x * kBWarps;                           \
+  (void)grp;
+
+template <typename T, int KP>
 __global__ void __launch_bounds__(kBThreads)
 bdot_kernel(int64_t n, int k, const T* a, const T* b, BRed red) {
-  const int lane = threadIdx.x & 31;
-  const int64_t rows_total = (int64_t)gridDim.x * kBWarps;
+  B_ROWS(KP);
   double s = 0.0;
-  if (lane < k)
-    for (int64_t row = (threadIdx.x >> 5) * (int64_t)gridDim.x + blockIdx.x; row < n; row += rows_total)
-      s = fma((double)a[row * k + lane], (double)b[row * k + lane], s);
-  b_reduce(red, s);
+  if (j < k)
+    for (int64_t wb = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; wb * GR < n;
+         wb += warps_total) {
+      const int64_t row = wb * GR + grp;
+      if (row < n) s = fma((double)a[row * k + j], (double)b[row * k + j], s);
+    }
+  b_reduce(red, b_fold<KP>(s));
 }
 
 // X += alpha_j P; R -= alpha_j AP; reduce r.r  (inactive RHS untouched)
-template <typename T>
+template <typename T, int KP>
 __global__ void __launch_bounds__(kBThreads)
 bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, const T* AP, BRed red) {
   if (*(volatile int*)&bs->any_active == 0) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t rows_total = (int64_t)gridDim.x * kBWarps;
-  const bool on = lane < k && bs->active[lane];
-  const T a = on ? (T)bs->alpha[lane] : T(0);
+  B_ROWS(KP);
+  const bool on = j < k && bs->active[j];
+  const T a = on ? (T)bs->alpha[j] : T(0);
   double s = 0.0;
-  for (int64_t row = (threadIdx.x >> 5) * (int64_t)gridDim.x + blockIdx.x; row < n; row += rows_total) {
-    if (lane < k) {
-      const int64_t idx = row * k + lane;
+  if (j < k)
+    for (int64_t wb = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; wb * GR < n;
+         wb += warps_total) {
+      const int64_t row = wb * GR + grp;
+      if (row >= n) continue;
+      const int64_t idx = row * k + j;
       T r = R[idx];
       if (on) {
         X[idx] = fma_bt<T>(a, P[idx], X[idx]);
@@ -253,22 +305,36 @@ bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, co
       }
       s = fma((double)r, (double)r, s);
     }
-  }
-  b_reduce(red, s);
+  b_reduce(red, b_fold<KP>(s));
 }
 
 // P = Z + beta_j P  (active RHS only)
-template <typename T>
+template <typename T, int KP>
 __global__ void __launch_bounds__(kBThreads)
 bxpay_kernel(int64_t n, int k, const BatchScalars* bs, const T* Zv, T* P) {
   if (*(volatile const int*)&bs->any_active == 0) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t rows_total = (int64_t)gridDim.x * kBWarps;
-  if (lane >= k || !bs->active[lane]) return;
-  const T b = (T)bs->beta[lane];
-  for (int64_t row = (threadIdx.x >> 5) * (int64_t)gridDim.x + blockIdx.x; row < n; row += rows_total) {
-    const int64_t idx = row * k + lane;
+  B_ROWS(KP);
+  if (j >= k || !bs->active[j]) return;
+  const T b = (T)bs->beta[j];
+  for (int64_t wb = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; wb * GR < n;
+       wb += warps_total) {
+    const int64_t row = wb * GR + grp;
+    if (row >= n) continue;
+    const int64_t idx = row * k + j;
     P[idx] = fma_bt<T>(b, P[idx], Zv[idx]);
+  }
+}
+
+// Calls f(std::integral_constant<int, KP>{}) for the group width of k.
+template <typename F>
+static void with_kp(int k, F&& f) {
+  switch (kp_for(k)) {
+    case 1: f(std::integral_constant<int, 1>{}); break;
+    case 2: f(std::integral_constant<int, 2>{}); break;
+    case 4: f(std::integral_constant<int, 4>{}); break;
+    case 8: f(std::integral_constant<int, 8>{}); break;
+    case 16: f(std::integral_constant<int, 16>{}); break;
+    default: f(std::integral_constant<int, 32>{}); break;
   }
 }
 
@@ -333,8 +399,10 @@ __global__ void mask_columns_kernel(int64_t n, int k, const int* mask, T* X) {
     if (mask[i % k]) X[i] = T(0);
 }
 
-int b_grid(int64_t nrow) {
-  const int64_t g = (nrow + kBWarps - 1) / kBWarps;
+// CTAs for nrow rows at 32/KP rows per warp (a function of k only through KP).
+int b_grid(int64_t nrow, int kp) {
+  const int64_t rows_per_cta = (int64_t)kBWarps * (32 / kp);
+  const int64_t g = (nrow + rows_per_cta - 1) / rows_per_cta;
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, kBMaxCtas));
 }
 
@@ -359,8 +427,10 @@ static int bcsr_copy(BCsr& m, int nrow, int ncol, const int32_t* off, const int3
 
 struct BOp {
   virtual ~BOp() = default;
+  size_t device_bytes = 0;  // DevBuf bytes held (declared first: released last)
   int64_t rows = 0;
   int vdtype = GBPC_F64;  // vector dtype
+  int max_rhs = kB;       // capacity of the scratch blocks
   virtual int apply(int k, const void* X, const void* Y, void* Z, double alpha, double beta,
                     const int* guard, const BRed* dot, cudaStream_t st) = 0;
 };
@@ -372,14 +442,18 @@ static void launch_bspmm(const BCsr& m, int k, const void* X, const void* Y, voi
   BRed red{};
   if (dot) red = *dot;
   const int az = alpha == 0.0, a1 = alpha == 1.0, bz = beta == 0.0;
-  if (dot && dot->w)
-    bspmm_kernel<V, T, EPI, true><<<b_grid(m.nrow), kBThreads, 0, st>>>(
-        m.nrow, k, m.off.as<int32_t>(), m.col.as<int32_t>(), m.val.as<V>(), (const T*)X,
-        (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard, red);
-  else
-    bspmm_kernel<V, T, EPI, false><<<b_grid(m.nrow), kBThreads, 0, st>>>(
-        m.nrow, k, m.off.as<int32_t>(), m.col.as<int32_t>(), m.val.as<V>(), (const T*)X,
-        (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard, red);
+  with_kp(k, [&](auto kpc) {
+    constexpr int KP = decltype(kpc)::value;
+    const int g = b_grid(m.nrow, KP);
+    if (dot && dot->w)
+      bspmm_kernel<V, T, EPI, true, KP><<<g, kBThreads, 0, st>>>(
+          m.nrow, k, m.off.as<int32_t>(), m.col.as<int32_t>(), m.val.as<V>(), (const T*)X,
+          (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard, red);
+    else
+      bspmm_kernel<V, T, EPI, false, KP><<<g, kBThreads, 0, st>>>(
+          m.nrow, k, m.off.as<int32_t>(), m.col.as<int32_t>(), m.val.as<V>(), (const T*)X,
+          (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard, red);
+  });
 }
 
 template <int EPI>
@@ -412,7 +486,7 @@ struct BSparseOp : BOp {
 
 struct BFsaiOp : BOp {
   BCsr g, gt;
-  DevBuf tmp;  // rows * 32 vectors
+  DevBuf tmp;  // rows * max_rhs vectors
   int apply(int k, const void* X, const void* Y, void* Z, double alpha, double beta,
             const int* guard, const BRed* dot, cudaStream_t st) override {
     int rc;
@@ -514,27 +588,44 @@ static int bcsr_copy(BCsr& m, int nrow, int ncol, const int32_t* off, const int3
 // Batched PCG (device loop in one CUDA graph, per-RHS stopping).
 
 struct BSolver {
+  size_t device_bytes = 0;  // DevBuf bytes held (declared first: released last)
   BOp* A = nullptr;
   BOp* M = nullptr;
   int64_t n = 0;
   int vdtype = GBPC_F32;
+  int max_rhs = kB;
   DevBuf R, Zv, P, AP, bs, partials, counter;
+  // Graph being built (moved into `graphs` once instantiated).
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphConditionalHandle handle = 0;
-  const void* last_b = nullptr;
-  void* last_x = nullptr;
-  int last_k = 0;
+  // Instantiated graphs by (B, X, k), least recently used dropped first.
+  struct Cached {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    cudaGraphConditionalHandle handle;
+    const void* b;
+    void* x;
+    int k;
+    uint64_t used;
+  };
+  static constexpr size_t kMaxGraphs = 8;
+  std::vector<Cached> graphs;
+  uint64_t clock = 0;
   int unroll = 8;
 
-  ~BSolver() { drop(); }
+  ~BSolver() {
+    drop();
+    for (auto& c : graphs) {
+      cudaGraphExecDestroy(c.exec);
+      cudaGraphDestroy(c.graph);
+    }
+  }
   void drop() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
     graph = nullptr;
-    last_b = nullptr;
-    last_x = nullptr;
   }
   BatchScalars* S() { return bs.as<BatchScalars>(); }
   BRed red(const void* w, int mode) {
@@ -553,7 +644,10 @@ struct BSolver {
     int rc;
     GBPC_CUDA_TRY(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), st));
     BRed rbb = red(B, BF_BB);
-    bdot_kernel<T><<<b_grid(n), kBThreads, 0, st>>>(n, k, (const T*)B, (const T*)B, rbb);
+    with_kp(k, [&](auto kpc) {
+      constexpr int KP = decltype(kpc)::value;
+      bdot_kernel<T, KP><<<b_grid(n, KP), kBThreads, 0, st>>>(n, k, (const T*)B, (const T*)B, rbb);
+    });
     GBPC_CUDA_TRY(cudaGetLastError());
     BRed rrr = red(R.p, BF_INIT_RR);
     if ((rc = A->apply(k, X, B, R.p, -1.0, 1.0, nullptr, &rrr, st))) return rc;
@@ -570,12 +664,18 @@ struct BSolver {
     BRed ra = red(P.p, BF_ALPHA);
     if ((rc = A->apply(k, P.p, nullptr, AP.p, 1.0, 0.0, guard, &ra, st))) return rc;
     BRed rr = red(R.p, BF_RR);
-    bcg_update_kernel<T><<<b_grid(n), kBThreads, 0, st>>>(n, k, S(), (T*)X, (T*)R.p,
-                                                           (const T*)P.p, (const T*)AP.p, rr);
+    with_kp(k, [&](auto kpc) {
+      constexpr int KP = decltype(kpc)::value;
+      bcg_update_kernel<T, KP><<<b_grid(n, KP), kBThreads, 0, st>>>(
+          n, k, S(), (T*)X, (T*)R.p, (const T*)P.p, (const T*)AP.p, rr);
+    });
     GBPC_CUDA_TRY(cudaGetLastError());
     BRed rb = red(R.p, BF_BETA);
     if ((rc = M->apply(k, R.p, nullptr, Zv.p, 1.0, 0.0, guard, &rb, st))) return rc;
-    bxpay_kernel<T><<<b_grid(n), kBThreads, 0, st>>>(n, k, S(), (const T*)Zv.p, (T*)P.p);
+    with_kp(k, [&](auto kpc) {
+      constexpr int KP = decltype(kpc)::value;
+      bxpay_kernel<T, KP><<<b_grid(n, KP), kBThreads, 0, st>>>(n, k, S(), (const T*)Zv.p, (T*)P.p);
+    });
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
   }
@@ -646,23 +746,40 @@ struct BSolver {
       cudaGetLastError();
       return rc;
     }
-    last_b = B;
-    last_x = X;
-    last_k = k;
+    if (graphs.size() >= kMaxGraphs) {
+      auto lru = std::min_element(graphs.begin(), graphs.end(),
+                                  [](const Cached& a, const Cached& b) { return a.used < b.used; });
+      cudaGraphExecDestroy(lru->exec);
+      cudaGraphDestroy(lru->graph);
+      graphs.erase(lru);
+    }
+    graphs.push_back(Cached{graph, exec, handle, B, X, k, ++clock});
+    graph = nullptr;
+    exec = nullptr;
     return GBPC_OK;
   }
 
   int run(int k, const void* B, void* X, double tol, double atol, int maxiter, int32_t* nit,
           double* rr, cudaStream_t st) {
     if (maxiter <= 0) maxiter = (int)std::min<int64_t>(n, 0x7fffffff);
+    if (k > max_rhs || k > A->max_rhs || k > M->max_rhs) {
+      gbpc_set_error("batched solver: %d right-hand sides exceed the capacity (%d)", k,
+                     std::min(max_rhs, std::min(A->max_rhs, M->max_rhs)));
+      return GBPC_ERR_ARG;
+    }
     int rc;
-    if (!exec || last_b != B || last_x != X || last_k != k) {
+    Cached* hit = nullptr;
+    for (auto& c : graphs)
+      if (c.b == B && c.x == X && c.k == k) hit = &c;
+    if (!hit) {
       rc = (vdtype == GBPC_F64) ? build<double>(k, B, X, st) : build<float>(k, B, X, st);
       if (rc) return rc;
+      hit = &graphs.back();
     }
-    bset_kernel<<<1, kB, 0, st>>>(S(), k, tol, atol, maxiter, (unsigned long long)handle);
+    hit->used = ++clock;
+    bset_kernel<<<1, kB, 0, st>>>(S(), k, tol, atol, maxiter, (unsigned long long)hit->handle);
     GBPC_CUDA_TRY(cudaGetLastError());
-    GBPC_CUDA_TRY(cudaGraphLaunch(exec, st));
+    GBPC_CUDA_TRY(cudaGraphLaunch(hit->exec, st));
     if (nit || rr) bcopy_outputs_kernel<<<1, kB, 0, st>>>(S(), k, nit, rr);
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
@@ -710,6 +827,7 @@ extern "C" int gbpc_bop_sparse(int n, const int32_t* off, const int32_t* col, co
   }
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new BSparseOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = n;
   op->vdtype = vector_dtype;
   rc = bcsr_copy(op->a, n, n, off, col, val, in_dtype, value_dtype, nullptr, st);
@@ -724,21 +842,23 @@ extern "C" int gbpc_bop_sparse(int n, const int32_t* off, const int32_t* col, co
 
 extern "C" int gbpc_bop_fsai(int n, const int32_t* g_off, const int32_t* g_col, const void* g_val,
                              const int32_t* gt_off, const int32_t* gt_col, const void* gt_val,
-                             int in_dtype, int value_dtype, int vector_dtype, void* stream,
-                             gbpc_bop** out) {
+                             int in_dtype, int value_dtype, int vector_dtype, int max_rhs,
+                             void* stream, gbpc_bop** out) {
   int rc = bop_vdtype_ok(value_dtype, vector_dtype);
   if (rc) return rc;
-  if (!out || n < 0 || !g_off || !gt_off) {
+  if (!out || n < 0 || !g_off || !gt_off || max_rhs < 1 || max_rhs > kB) {
     gbpc_set_error("gbpc_bop_fsai: bad arguments");
     return GBPC_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new BFsaiOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = n;
   op->vdtype = vector_dtype;
+  op->max_rhs = max_rhs;
   rc = bcsr_copy(op->g, n, n, g_off, g_col, g_val, in_dtype, value_dtype, nullptr, st);
   if (!rc) rc = bcsr_copy(op->gt, n, n, gt_off, gt_col, gt_val, in_dtype, value_dtype, nullptr, st);
-  if (!rc) rc = op->tmp.alloc(dtype_size(vector_dtype) * std::max(n, 1) * kB);
+  if (!rc) rc = op->tmp.alloc(dtype_size(vector_dtype) * std::max(n, 1) * max_rhs);
   if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = GBPC_ERR_CUDA;
   if (rc) {
     delete op;
@@ -758,10 +878,11 @@ __global__ void bsqlap_prep_kernel(int n, const double* mass, double w, T* inv, 
 
 extern "C" int gbpc_bop_sqlap(int n, const int32_t* off, const int32_t* col, const void* val,
                               int in_dtype, int value_dtype, int vector_dtype, const double* mass,
-                              double mass_weight, void* stream, gbpc_bop** out) {
+                              double mass_weight, int max_rhs, void* stream, gbpc_bop** out) {
   int rc = bop_vdtype_ok(value_dtype, vector_dtype);
   if (rc) return rc;
-  if (!out || n < 0 || !off || !mass || !std::isfinite(mass_weight) || mass_weight < 0) {
+  if (!out || n < 0 || !off || !mass || !std::isfinite(mass_weight) || mass_weight < 0 ||
+      max_rhs < 1 || max_rhs > kB) {
     gbpc_set_error("gbpc_bop_sqlap: bad arguments");
     return GBPC_ERR_ARG;
   }
@@ -771,8 +892,10 @@ extern "C" int gbpc_bop_sqlap(int n, const int32_t* off, const int32_t* col, con
   }
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new BSqlapOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = n;
   op->vdtype = vector_dtype;
+  op->max_rhs = max_rhs;
   DevBuf inv64, wm64;
   rc = inv64.alloc(sizeof(double) * std::max(n, 1));
   if (!rc) rc = op->wmass.alloc(dtype_size(vector_dtype) * std::max(n, 1));
@@ -788,7 +911,7 @@ extern "C" int gbpc_bop_sqlap(int n, const int32_t* off, const int32_t* col, con
   // Forward matrix M^-1 L (rows scaled in float64 before narrowing), backward L.
   if (!rc) rc = bcsr_copy(op->fwd, n, n, off, col, val, GBPC_F64, value_dtype, inv64.p, st);
   if (!rc) rc = bcsr_copy(op->bwd, n, n, off, col, val, GBPC_F64, value_dtype, nullptr, st);
-  if (!rc) rc = op->tmp.alloc(dtype_size(vector_dtype) * std::max(n, 1) * kB);
+  if (!rc) rc = op->tmp.alloc(dtype_size(vector_dtype) * std::max(n, 1) * max_rhs);
   if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = GBPC_ERR_CUDA;
   if (rc) {
     delete op;
@@ -800,8 +923,8 @@ extern "C" int gbpc_bop_sqlap(int n, const int32_t* off, const int32_t* col, con
 
 extern "C" int gbpc_bop_apply(gbpc_bop* op, int k, const void* X, const void* Y, void* Z,
                               double alpha, double beta, void* stream) {
-  if (!op || k < 1 || k > kB) {
-    gbpc_set_error("gbpc_bop_apply: k must be 1..32");
+  if (!op || k < 1 || k > op->impl->max_rhs) {
+    gbpc_set_error("gbpc_bop_apply: k must be 1..%d", op ? op->impl->max_rhs : kB);
     return GBPC_ERR_ARG;
   }
   if (X == Z && alpha != 0.0) {
@@ -811,6 +934,15 @@ extern "C" int gbpc_bop_apply(gbpc_bop* op, int k, const void* X, const void* Y,
   return op->impl->apply(k, X, Y, Z, alpha, beta, nullptr, nullptr, (cudaStream_t)stream);
 }
 
+extern "C" int gbpc_bop_device_bytes(const gbpc_bop* op, size_t* bytes_host) {
+  if (!op || !bytes_host) {
+    gbpc_set_error("gbpc_bop_device_bytes: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *bytes_host = op->impl->device_bytes;
+  return GBPC_OK;
+}
+
 extern "C" int gbpc_bop_destroy(gbpc_bop* op) {
   if (!op) return GBPC_OK;
   cudaDeviceSynchronize();
@@ -818,21 +950,27 @@ extern "C" int gbpc_bop_destroy(gbpc_bop* op) {
   return GBPC_OK;
 }
 
-extern "C" int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, void* stream,
-                                   gbpc_bsolver** out) {
+extern "C" int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, int max_rhs,
+                                   void* stream, gbpc_bsolver** out) {
   if (!out || !A || !M || A->impl->rows != M->impl->rows || A->impl->vdtype != M->impl->vdtype) {
     gbpc_set_error("gbpc_bsolver_create: operator and preconditioner must match in size and "
                    "vector dtype");
     return GBPC_ERR_ARG;
   }
+  if (max_rhs < 1 || max_rhs > kB) {
+    gbpc_set_error("gbpc_bsolver_create: max_rhs must be 1..%d", kB);
+    return GBPC_ERR_ARG;
+  }
   auto* h = new gbpc_bsolver;
   BSolver& s = h->s;
+  ByteTally tally(&s.device_bytes);
+  s.max_rhs = max_rhs;
   s.A = A->impl.get();
   s.M = M->impl.get();
   s.n = A->impl->rows;
   s.vdtype = A->impl->vdtype;
   if (unroll > 0) s.unroll = std::min(unroll, 64);
-  const size_t bytes = dtype_size(s.vdtype) * std::max<int64_t>(s.n, 1) * kB;
+  const size_t bytes = dtype_size(s.vdtype) * std::max<int64_t>(s.n, 1) * max_rhs;
   int rc = s.R.alloc(bytes);
   if (!rc) rc = s.Zv.alloc(bytes);
   if (!rc) rc = s.P.alloc(bytes);
@@ -854,11 +992,20 @@ extern "C" int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, void* s
 extern "C" int gbpc_bsolver_run(gbpc_bsolver* h, int k, const void* B, void* X, double tol,
                                 double atol, int maxiter, int32_t* nit_dev, double* rr_dev,
                                 void* stream) {
-  if (!h || k < 1 || k > kB || !B || !X) {
-    gbpc_set_error("gbpc_bsolver_run: bad arguments (k must be 1..32)");
+  if (!h || k < 1 || k > h->s.max_rhs || !B || !X) {
+    gbpc_set_error("gbpc_bsolver_run: bad arguments (k must be 1..%d)", h ? h->s.max_rhs : kB);
     return GBPC_ERR_ARG;
   }
   return h->s.run(k, B, X, tol, atol, maxiter, nit_dev, rr_dev, (cudaStream_t)stream);
+}
+
+extern "C" int gbpc_bsolver_device_bytes(const gbpc_bsolver* h, size_t* bytes_host) {
+  if (!h || !bytes_host) {
+    gbpc_set_error("gbpc_bsolver_device_bytes: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *bytes_host = h->s.device_bytes;
+  return GBPC_OK;
 }
 
 extern "C" int gbpc_bsolver_destroy(gbpc_bsolver* h) {
@@ -876,8 +1023,8 @@ extern "C" int gbpc_bsolver_destroy(gbpc_bsolver* h) {
 extern "C" int gbpc_refine(gbpc_bop* A64, gbpc_bsolver* inner, int k, const double* B, double* X,
                            double tol_outer, double tol_inner, int max_outer, int max_inner,
                            int32_t* outer_host, int32_t* inner_host, void* stream) {
-  if (!A64 || !inner || k < 1 || k > kB || !B || !X || A64->impl->vdtype != GBPC_F64 ||
-      A64->impl->rows != inner->s.n) {
+  if (!A64 || !inner || k < 1 || k > kB || k > A64->impl->max_rhs || !B || !X ||
+      A64->impl->vdtype != GBPC_F64 || A64->impl->rows != inner->s.n) {
     gbpc_set_error("gbpc_refine: bad arguments");
     return GBPC_ERR_ARG;
   }

@@ -16,18 +16,39 @@ constexpr int kMaxCtas = 152 * 8;  // partial-sum capacity of every reduction bu
 size_t dtype_size(int dtype);
 bool valid_value_dtype(int d);
 
+// Bookkeeping of device bytes held by DevBuf allocations: a process-wide
+// live total, and per object a tally.  While a ByteTally scope is open on a
+// thread, every DevBuf that thread allocates adds its bytes to the scope's
+// counter and takes them back when released, so an operator or solver built
+// inside such a scope knows the device bytes it holds.
+void note_release(size_t bytes, size_t* tally);
+size_t* current_tally();
+size_t device_bytes_live();
+struct ByteTally {
+  size_t* prev;
+  explicit ByteTally(size_t* counter);
+  ~ByteTally();
+  ByteTally(const ByteTally&) = delete;
+  ByteTally& operator=(const ByteTally&) = delete;
+};
+
 // Owned device allocation.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  size_t* tally = nullptr;  // counter charged with `bytes` (nullable)
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      note_release(bytes, tally);
+    }
     p = nullptr;
     bytes = 0;
+    tally = nullptr;
   }
   int alloc(size_t n);
   template <typename T> T* as() const { return static_cast<T*>(p); }
@@ -117,6 +138,7 @@ int vec_copy(void* dst, const void* src, size_t bytes, cudaStream_t st);
 
 struct Operator {
   virtual ~Operator() = default;
+  size_t device_bytes = 0;  // DevBuf bytes held (declared first: released last)
   int64_t rows = 0;        // scalar vector length
   int vdtype = GBPC_F64;   // vector dtype
   // z = alpha Op x + beta y.  `guard` (nullable device int) skips all work

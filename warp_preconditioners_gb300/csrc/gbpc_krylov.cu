@@ -115,6 +115,7 @@ int vec_grid(int64_t n) { return std::min<int64_t>(grid_for(n, kThreads), kSms *
 }  // namespace
 
 struct Solver {
+  size_t device_bytes = 0;  // DevBuf bytes held (declared first: released last)
   int method = GBPC_CG;
   Operator* A = nullptr;
   Operator* M = nullptr;
@@ -395,6 +396,7 @@ extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_gr
   }
   auto* h = new gbpc_solver;
   Solver& s = h->s;
+  ByteTally tally(&s.device_bytes);
   s.method = method;
   s.A = a;
   s.M = m;
@@ -428,6 +430,15 @@ extern "C" int gbpc_solver_run(gbpc_solver* h, const double* b, double* x, doubl
     return GBPC_ERR_ARG;
   }
   return h->s.run(b, x, tol, atol, maxiter, nit_dev, rr_dev, atol_sq_dev, (cudaStream_t)stream);
+}
+
+extern "C" int gbpc_solver_device_bytes(const gbpc_solver* h, size_t* bytes_host) {
+  if (!h || !bytes_host) {
+    gbpc_set_error("gbpc_solver_device_bytes: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *bytes_host = h->s.device_bytes;
+  return GBPC_OK;
 }
 
 extern "C" int gbpc_solver_destroy(gbpc_solver* h) {

@@ -343,6 +343,7 @@ extern "C" int gbpc_op_sparse(int nrow, int ncol, int block, const int32_t* offs
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new SparseOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = (int64_t)nrow * block;
   op->vdtype = vector_dtype;
   rc = sell_build(op->m, nrow, ncol, block, offsets, columns, values, value_dtype, value_dtype,
@@ -375,6 +376,7 @@ extern "C" int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new FsaiOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = (int64_t)nrow * block;
   op->vdtype = vector_dtype;
   const int in = input_dtype(value_dtype);
@@ -416,6 +418,7 @@ extern "C" int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* colum
   }
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new SqlapOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = nfree;
   op->vdtype = dtype;
   op->n = n;
@@ -523,6 +526,7 @@ extern "C" int gbpc_op_diagonal(int nrow, int block, const int32_t* offsets,
   }
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new DiagOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = (int64_t)nrow * block;
   op->vdtype = dtype;
   DevBuf tmp;
@@ -567,6 +571,7 @@ extern "C" int gbpc_op_block_jacobi(int nrow, int block, const int32_t* offsets,
   }
   cudaStream_t st = (cudaStream_t)stream;
   auto* op = new BlockJacobiOp;
+  ByteTally tally(&op->device_bytes);
   op->rows = (int64_t)nrow * block;
   op->vdtype = dtype;
   op->nrow = nrow;
@@ -632,6 +637,7 @@ extern "C" int gbpc_op_bilu0(int nrow, int block, const int32_t* offsets, const 
   const size_t vs = dtype_size(dtype);
   const int bb = block * block;
   auto* op = new Bilu0Op;
+  ByteTally tally(&op->device_bytes);
   op->rows = (int64_t)nrow * block;
   op->vdtype = dtype;
   op->nrow = nrow;
@@ -684,6 +690,15 @@ extern "C" int gbpc_op_apply(gbpc_op* h, const void* x, const void* y, void* z, 
     x = op->alias_scratch.p;
   }
   return op->apply(x, y, z, alpha, beta, nullptr, nullptr, st);
+}
+
+extern "C" int gbpc_op_device_bytes(const gbpc_op* h, size_t* bytes_host) {
+  if (!h || !h->impl || !bytes_host) {
+    gbpc_set_error("gbpc_op_device_bytes: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *bytes_host = h->impl->device_bytes;
+  return GBPC_OK;
 }
 
 extern "C" int gbpc_op_rows(const gbpc_op* h, int64_t* rows_host) {

@@ -6,6 +6,7 @@
 // instruction has all lanes busy (FP64 is the scarce unit on GB300); the row
 // sum uses two interleaved accumulators to halve the dependent-FMA chain.
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
@@ -39,6 +40,15 @@ void gbpc_set_error_cuda(cudaError_t e, const char* expr, const char* file, int 
 extern "C" const char* gbpc_last_error(void) { return g_last_error.c_str(); }
 extern "C" int gbpc_version(void) { return 1; }
 
+extern "C" int gbpc_device_bytes(size_t* live_host) {
+  if (!live_host) {
+    gbpc_set_error("gbpc_device_bytes: null output");
+    return GBPC_ERR_ARG;
+  }
+  *live_host = gbpc::device_bytes_live();
+  return GBPC_OK;
+}
+
 namespace gbpc {
 
 size_t dtype_size(int dtype) {
@@ -52,6 +62,22 @@ size_t dtype_size(int dtype) {
 
 bool valid_value_dtype(int d) { return d == GBPC_F64 || d == GBPC_F32 || d == GBPC_BF16; }
 
+namespace {
+std::atomic<size_t> g_live_bytes{0};
+thread_local size_t* t_tally = nullptr;
+}  // namespace
+
+size_t* current_tally() { return t_tally; }
+size_t device_bytes_live() { return g_live_bytes.load(); }
+
+void note_release(size_t n, size_t* tally) {
+  g_live_bytes.fetch_sub(n);
+  if (tally) *tally -= n;
+}
+
+ByteTally::ByteTally(size_t* counter) : prev(t_tally) { t_tally = counter; }
+ByteTally::~ByteTally() { t_tally = prev; }
+
 int DevBuf::alloc(size_t n) {
   release();
   if (n == 0) n = 16;
@@ -62,6 +88,9 @@ int DevBuf::alloc(size_t n) {
     return GBPC_ERR_NOMEM;
   }
   bytes = n;
+  tally = t_tally;
+  if (tally) *tally += n;
+  g_live_bytes.fetch_add(n);
   return GBPC_OK;
 }
 

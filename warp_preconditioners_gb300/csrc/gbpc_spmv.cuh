@@ -35,7 +35,7 @@ enum SpmvFlags : int { F_ALPHA_ZERO = 1, F_ALPHA_ONE = 2, F_BETA_ZERO = 4 };
 template <int B> struct Chunk { static constexpr int value = 8; };
 template <> struct Chunk<2> { static constexpr int value = 4; };
 template <> struct Chunk<3> { static constexpr int value = 2; };
-template <> struct Chunk<4> { static constexpr int value = 2; };
+template <> struct Chunk<4> { static constexpr int value = 1; };
 
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB)
@@ -139,12 +139,15 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
 
 // Launch configuration of a variant: CTAs resident per SM times SMs, with
 // slices spread over the warps by a grid stride.
-static int spmv_grid(int nslices, int minb) {
+// Every variant launches the same grid (one 1024-thread CTA per SM at most),
+// so the CTA partials of a fused dot product, and therefore its rounding, do
+// not depend on which variant the autotuner picked: results are identical
+// whatever the timing (and whatever else shares the GPU).
+static int spmv_grid(int nslices, int /*minb*/) {
   const int warps_per_cta = kThreads / 32;
   int g = (nslices + warps_per_cta - 1) / warps_per_cta;
-  const int cap = kSms * minb;
   if (g < 1) g = 1;
-  if (g > cap) g = cap;
+  if (g > kSms) g = kSms;
   return g;
 }
 
@@ -156,9 +159,9 @@ static int spmv_flags(double alpha, double beta) {
   return f;
 }
 
-// Product kernel variants for scalar rows: (entries loaded per chunk,
-// minimum resident 1024-thread CTAs per SM, i.e. a 32 or 64 register budget).
-// Blocked rows use one variant.
+// Product kernel variants for scalar rows differ in the entries loaded per
+// chunk (8, 16, 4); all have a 64-register budget (one 1024-thread CTA per
+// SM).  Blocked rows use one variant.
 constexpr int kNumVariants = 3;
 
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
@@ -181,17 +184,15 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
                                              nslices, st);
         return;
       case 2:
-        launch_one<B, V, A, EPI, DOT, 4, 2>(view, x, y, z, alpha, beta, flags, guard, e, red,
+        launch_one<B, V, A, EPI, DOT, 4, 1>(view, x, y, z, alpha, beta, flags, guard, e, red,
                                             nslices, st);
         return;
       default:
         break;
     }
   }
-  // Blocked rows hold B*B values per entry: give them the 64-register budget.
-  constexpr int minb = (B == 1) ? kCtasPerSm : 1;
-  launch_one<B, V, A, EPI, DOT, Chunk<B>::value, minb>(view, x, y, z, alpha, beta, flags, guard, e,
-                                                       red, nslices, st);
+  launch_one<B, V, A, EPI, DOT, Chunk<B>::value, 1>(view, x, y, z, alpha, beta, flags, guard, e,
+                                                    red, nslices, st);
 }
 
 template <int B, typename V, typename A, int EPI>

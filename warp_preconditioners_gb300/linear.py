@@ -120,6 +120,11 @@ class Solver:
             except Exception:
                 pass
 
+    @property
+    def device_bytes(self) -> int:
+        """Device bytes of the Krylov state (work vectors and scalars)."""
+        return _lib.object_bytes("gbpc_solver_device_bytes", self._h)
+
     def run(self, b, x, tol=None, atol=None, maxiter=0):
         tol = 1.0e-5 if tol is None else float(tol)
         atol = 0.0 if atol is None else float(atol)
