@@ -386,6 +386,7 @@ def main():
         line["e2e"] = run_e2e(args, prob, dev, one_step, world, dist)
     if not args.no_mixed:
         line["mixed_batched"] = run_mixed_batched(args, prob, Q, K, mass, free, dev)
+    line["refit"] = measure_refit(args, prob, Q, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline_sample(prob, args.width, args.step_size, args.method, args.cpu_iters,
                                  iters[-1])
@@ -507,6 +508,43 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
     }
 
 
+def measure_refit(args, prob, Q, dev):
+    """Fixed-support numeric refit (FSAI.update, fsai_reuse.py) against a full
+    adaptive setup: the refit takes Q with alpha doubled (same pattern, new
+    values; host assembly untimed).  CUDA-event medians of 3."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, from_scipy, problems
+
+    Q2 = from_scipy(problems.biharmonic(prob["K"], prob["mass"], 2 * ALPHA), dev)
+
+    def timed(fn):
+        out = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return statistics.median(out)
+
+    kw = dict(max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+    setup_ms = timed(lambda: FSAI(Q, **kw))
+    pre = FSAI(Q, reuse_pattern=True, **kw)
+    mats = [Q2, Q]
+    state = {"i": 0}
+
+    def refit():
+        pre.update(mats[state["i"] % 2])
+        state["i"] += 1
+
+    refit_ms = timed(refit)
+    return {"matrix": f"Q with alpha {ALPHA:g} -> {2 * ALPHA:g} (same pattern)",
+            "setup_ms": setup_ms, "refit_ms": refit_ms, "setup_over_refit": setup_ms / refit_ms}
+
+
 def run_c3(args, dev, maxiter=20000):
     """K (x) C block coupling: K = 7-point Dirichlet Laplacian on an n^3 grid,
     C = R diag(1, 1, 1e-6) R^T with a seeded rotation, 3x3 blocks, float64;
@@ -621,19 +659,23 @@ def run_c5(args, dev):
     # max_i |b - A x|_i / (|A| |x| + |b|)_i.  For the alpha = 1e-4 biharmonic
     # systems the first is dominated by cancellation in forming b - A x
     # (|A| |x| >> |b|); the second is the accuracy measure.
-    worst_rel = worst_berr = 0.0
+    rel, berr, nonfinite = [], [], 0
     for req, r in zip(stream, served):
         if r.ok and r.x is not None:
             h = cat.get(req.key)
             A = h.A if h.kind == "laplacian" else h.P
             b, x = serve.request_rhs(req).numpy(), r.x.numpy()
+            if not np.isfinite(x).all():
+                nonfinite += 1
+                continue
             res = b - A @ x
-            worst_rel = max(worst_rel, float((np.linalg.norm(res, axis=0)
-                                              / np.linalg.norm(b, axis=0)).max()))
+            rel.append(float((np.linalg.norm(res, axis=0) / np.linalg.norm(b, axis=0)).max()))
             den = abs(A) @ np.abs(x) + np.abs(b)
-            worst_berr = max(worst_berr, float((np.abs(res) / den).max()))
-    out["served"]["relres_max_sampled"] = worst_rel
-    out["served"]["backward_error_max_sampled"] = worst_berr
+            berr.append(float((np.abs(res) / den).max()))
+    out["served"]["checked_requests"] = len(rel) + nonfinite
+    out["served"]["nonfinite_solutions"] = nonfinite
+    out["served"]["relres_max_sampled"] = max(rel) if rel else None
+    out["served"]["backward_error_max_sampled"] = max(berr) if berr else None
 
     if not args.c5_no_sequential:
         seq_ex = serve.GpuExecutor(cat, sequential=True, tol=args.rtol, device=dev)

@@ -115,6 +115,33 @@ int gbpc_convert_factor(int n, const int32_t* offsets, const int32_t* columns, c
                         int src_dtype, void* dst, int dst_dtype, int32_t* invalid_host,
                         void* stream);
 
+/* Fixed-support numeric refit.  Replaces RefitPlan.update's `diagonal` +
+ * `refit` launches (warp_preconditioners/fsai_reuse.py:75-149, :189-245):
+ * for every row i of G (CSR g_off/g_col, sorted, diagonal last, at most
+ * `width` entries) the local Cholesky of the Jacobi-scaled A on G's support
+ * is solved for e_i and normalised, written to out[nnz(G)] in factor_dtype
+ * (matrix float64 -> factor float64 / float32 / bfloat16; float32 ->
+ * float32 / bfloat16).  G itself is not touched.  status_host[0] counts
+ * non-finite or non-positive diagonals of A, status_host[1] rows with a
+ * pivot <= pivot_floor, a non-finite value or a non-positive diagonal; the
+ * caller publishes `out` only when both are zero.  Synchronises. */
+int gbpc_fsai_refit(int n, const int32_t* a_off, const int32_t* a_col, const void* a_val,
+                    int dtype, const int32_t* g_off, const int32_t* g_col, int width,
+                    double pivot_floor, void* out, int factor_dtype, int32_t* status_host,
+                    void* stream);
+
+/* map_out[e] = position in the transpose (t_offsets/t_columns) of entry e of
+ * the CSR matrix: replaces fsai_reuse.py `transpose_map` (:54-63).
+ * GBPC_ERR_ARG if an entry has no transposed counterpart.  Synchronises. */
+int gbpc_transpose_map(int nrow, const int32_t* offsets, const int32_t* columns,
+                       const int32_t* t_offsets, const int32_t* t_columns, int32_t* map_out,
+                       void* stream);
+
+/* dst[map[e]] = src[e] for e < count (map[e] < 0 skipped): fsai_reuse.py
+ * `transpose` (:151-155). */
+int gbpc_scatter_values(int64_t count, const void* src, const int32_t* map, void* dst, int dtype,
+                        void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Linear operators                                                          */
 /* ------------------------------------------------------------------------ */
@@ -138,6 +165,12 @@ int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int32_t* g_col
                  const void* g_val, const int32_t* gt_off, const int32_t* gt_col,
                  const void* gt_val, int value_dtype, int vector_dtype, void* stream,
                  gbpc_op** out);
+/* New values of G and G^T (same patterns as at creation) for an FSAI
+ * operator, written in place so that captured applies use them (the
+ * reference's refit keeps G.values and GT.values pointers). */
+int gbpc_op_fsai_refill(gbpc_op* op, const int32_t* g_off, const int32_t* g_col,
+                        const void* g_val, const int32_t* gt_off, const int32_t* gt_col,
+                        const void* gt_val, int value_dtype, void* stream);
 
 /* Factored (L diag(1/mass) L + mass_weight diag(mass))[free, free].
  * Replaces SquaredLaplacianOperator (warp_preconditioners/
@@ -169,6 +202,14 @@ int gbpc_op_diagonal(int nrow, int block, const int32_t* offsets, const int32_t*
 int gbpc_op_block_jacobi(int nrow, int block, const int32_t* offsets, const int32_t* columns,
                          const void* values, int dtype, double pivot_tolerance,
                          void* inverse_out, void* stream, gbpc_op** out);
+/* New values for a BlockJacobi operator, in place (BlockJacobi.update,
+ * warp_preconditioners/block_ilu.py:282-317): inverses are formed in a
+ * candidate buffer and copied over the operator's (and inverse_out) only
+ * when every pivot is valid; otherwise GBPC_ERR_PIVOT and nothing changes.
+ * Captured applies see the new inverse.  Synchronises. */
+int gbpc_op_block_jacobi_update(gbpc_op* op, int nrow, int block, const int32_t* offsets,
+                                const int32_t* columns, const void* values, int dtype,
+                                double pivot_tolerance, void* inverse_out, void* stream);
 
 /* Synchronous block ILU(0) with Jacobi triangular sweeps.  Replaces BlockILU0
  * (warp_preconditioners/block_ilu.py:347-450): `topology`, `invert`,

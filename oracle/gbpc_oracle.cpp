@@ -900,6 +900,83 @@ double dot(int n, const double* a, const double* b) {
 
 }  // namespace
 
+namespace {
+
+// warp_preconditioners/fsai_reuse.py:18-31 (`find`): slot of column j in the
+// sorted CSR row i, or -1.
+inline int find_slot(const int32_t* off, const int32_t* col, int i, int j) {
+  int lo = off[i], hi = off[i + 1];
+  const int end = hi;
+  while (lo < hi) {
+    const int mid = (lo + hi) / 2;
+    if (col[mid] < j) lo = mid + 1; else hi = mid;
+  }
+  return (lo < end && col[lo] == j) ? lo : -1;
+}
+
+// warp_preconditioners/fsai_reuse.py:75-149 (`refit`): on each row's fixed
+// support, the row-by-row Cholesky of the Jacobi-scaled local matrix, a
+// forward and a backward substitution for the unit vector of the row, and
+// the normalisation z / sqrt(z_i) * s.  Returns the number of invalid rows
+// (pivot <= floor or non-finite, non-finite value, non-positive diagonal).
+template <typename T, typename S>
+int32_t fsai_refit(int n, const int32_t* off, const int32_t* col, const T* val, const T* scale,
+                   const int32_t* goff, const int32_t* gcol, T floor_, S* out) {
+  int32_t bad = 0;
+#pragma omp parallel for reduction(+ : bad) schedule(dynamic, 64)
+  for (int i = 0; i < n; ++i) {
+    const int start = goff[i];
+    const int size = goff[i + 1] - start;
+    if (size < 1) {
+      bad += 1;
+      continue;
+    }
+    std::vector<T> chol((size_t)size * size, T(0)), z(size, T(0));
+    bool valid = true;
+    for (int p = 0; p < size; ++p) {
+      const int r = gcol[start + p];
+      for (int q = 0; q <= p; ++q) {
+        const int c = gcol[start + q];
+        const int slot = find_slot(off, col, r, c);
+        T a = T(0);
+        if (slot >= 0) a = val[slot] * scale[r] * scale[c];
+        for (int k = 0; k < q; ++k) a -= chol[(size_t)p * size + k] * chol[(size_t)q * size + k];
+        if (p == q) {
+          if (a <= floor_ || !finite(a)) {
+            valid = false;
+            a = T(1);
+          }
+          chol[(size_t)p * size + q] = std::sqrt(a);
+        } else {
+          chol[(size_t)p * size + q] = a / chol[(size_t)q * size + q];
+        }
+      }
+    }
+    for (int p = 0; p < size; ++p) {
+      T a = (gcol[start + p] == i) ? T(1) : T(0);
+      for (int q = 0; q < p; ++q) a -= chol[(size_t)p * size + q] * z[q];
+      z[p] = a / chol[(size_t)p * size + p];
+    }
+    for (int rev = 0; rev < size; ++rev) {
+      const int p = size - 1 - rev;
+      T a = z[p];
+      for (int q = p + 1; q < size; ++q) a -= chol[(size_t)q * size + p] * z[q];
+      z[p] = a / chol[(size_t)p * size + p];
+    }
+    const T norm = std::sqrt(z[size - 1]);
+    for (int p = 0; p < size; ++p) {
+      const S value = S(z[p] / norm * scale[gcol[start + p]]);
+      out[start + p] = value;
+      if (!finite(value)) valid = false;
+      if (p == size - 1 && value <= S(0)) valid = false;
+    }
+    if (!valid) bad += 1;
+  }
+  return bad;
+}
+
+}  // namespace
+
 extern "C" {
 
 int or_num_threads() {
@@ -1113,4 +1190,28 @@ void or_operator_apply(const Operator* op, const double* x, const double* y, dou
   op_apply(*op, x, y, z, alpha, beta, tmp);
 }
 
+
+void or_fsai_diagonal_f64(int n, const int32_t* off, const int32_t* col, const double* val,
+                          double* scale, int32_t* status) {
+  fsai_diagonal<double>(n, off, col, val, scale, status);
+}
+void or_fsai_diagonal_f32(int n, const int32_t* off, const int32_t* col, const float* val,
+                          float* scale, int32_t* status) {
+  fsai_diagonal<float>(n, off, col, val, scale, status);
+}
+int32_t or_fsai_refit_f64_f64(int n, const int32_t* off, const int32_t* col, const double* val,
+                              const double* scale, const int32_t* goff, const int32_t* gcol,
+                              double floor_, double* out) {
+  return fsai_refit<double, double>(n, off, col, val, scale, goff, gcol, floor_, out);
+}
+int32_t or_fsai_refit_f64_f32(int n, const int32_t* off, const int32_t* col, const double* val,
+                              const double* scale, const int32_t* goff, const int32_t* gcol,
+                              double floor_, float* out) {
+  return fsai_refit<double, float>(n, off, col, val, scale, goff, gcol, floor_, out);
+}
+int32_t or_fsai_refit_f32_f32(int n, const int32_t* off, const int32_t* col, const float* val,
+                              const float* scale, const int32_t* goff, const int32_t* gcol,
+                              float floor_, float* out) {
+  return fsai_refit<float, float>(n, off, col, val, scale, goff, gcol, floor_, out);
+}
 }  // extern "C"

@@ -173,6 +173,28 @@ def fsai(a: CSR, width=8, step=1, tol=1e-3, pivot_floor=None, factor_dtype=None)
     return g, transpose(g), int(status[1])
 
 
+def fsai_refit(a: CSR, g: CSR, pivot_floor=None, factor_dtype=None):
+    """fsai_reuse.py:189-245 (RefitPlan.update: `diagonal` then `refit`) on the
+    fixed supports of G.  Returns (values in G's layout, invalid diagonals,
+    invalid rows); the caller publishes the values only when both are 0."""
+    dtype = a.values.dtype
+    if pivot_floor is None:
+        pivot_floor = 1e-12 if dtype == np.float64 else 1e-6
+    out_dtype = np.dtype(factor_dtype) if factor_dtype is not None else dtype
+    n = a.nrow
+    scale = np.empty(max(n, 1), dtype)
+    status = np.zeros(1, np.int32)
+    getattr(lib(), "or_fsai_diagonal_" + _sfx(dtype))(
+        n, _p(a.offsets), _p(a.columns), _p(a.values), _p(scale), _p(status))
+    out = np.empty(max(len(g.columns), 1), out_dtype)
+    fn = getattr(lib(), f"or_fsai_refit_{_sfx(dtype)}_{_sfx(out_dtype)}")
+    fn.restype = ctypes.c_int32
+    bad = fn(n, _p(a.offsets), _p(a.columns), _p(a.values), _p(scale),
+             _p(np.ascontiguousarray(g.offsets, np.int32)),
+             _p(np.ascontiguousarray(g.columns, np.int32)), _scalar(dtype, pivot_floor), _p(out))
+    return out[:len(g.columns)], int(status[0]), int(bad)
+
+
 def csr_spmv(a: CSR, x, y, alpha, beta, accum_dtype=None):
     accum_dtype = np.dtype(accum_dtype or a.values.dtype)
     x = np.ascontiguousarray(x, accum_dtype)

@@ -138,7 +138,8 @@ def test_zero_tolerance_full_width(golden):
     np.testing.assert_allclose(g.T @ g, d["inv32"], rtol=1e-12, atol=1e-15)
 
 
-@pytest.mark.parametrize("width,step", [(8, 1), (8, 2), (48, 1), (48, 2), (64, 3)])
+@pytest.mark.parametrize("width,step", [(8, 1), (8, 2), (12, 2), (16, 1), (16, 3), (48, 1),
+                                        (48, 2), (64, 3)])
 def test_biharmonic_tet_cube_bit_exact(oracle, width, step):
     # The assembled smoothing operator of the benchmark, on a small cube:
     # 65-entry rows, exact ties, numerically nonsymmetric SpGEMM values.
@@ -148,6 +149,24 @@ def test_biharmonic_tet_cube_bit_exact(oracle, width, step):
     q = problems.biharmonic(K, mass, 1e-4)
     pre = FSAI(to_bsr(q), max_row_size=width, max_step_size=step, kap_tolerance=1e-3)
     g_or, gt_or, trunc = oracle.fsai(oracle_csr(oracle, q), width=width, step=step, tol=1e-3)
+    assert pre.truncated_rows == trunc
+    assert_same_factor(pre.G, g_or)
+    assert_same_factor(pre.GT, gt_or)
+
+
+@pytest.mark.parametrize("width,step", [(8, 2), (16, 2)])
+def test_wide_frontier_overflow_rerun_bit_exact(oracle, width, step):
+    # ~160 entries per row: frontiers exceed the first pass's candidate
+    # table, so those rows are rebuilt by the rerun with a larger table.
+    from warp_preconditioners_gb300 import FSAI
+
+    rng = np.random.default_rng(83)
+    n = 400
+    m = ss.random(n, n, density=0.2, random_state=rng, data_rvs=lambda k: rng.uniform(-1, 1, k))
+    a = (m + m.T).tocsr()
+    a = a + ss.diags(np.abs(a).sum(axis=1).A1 + 1.0)
+    pre = FSAI(to_bsr(a), max_row_size=width, max_step_size=step, kap_tolerance=0.0)
+    g_or, gt_or, trunc = oracle.fsai(oracle_csr(oracle, a), width=width, step=step, tol=0.0)
     assert pre.truncated_rows == trunc
     assert_same_factor(pre.G, g_or)
     assert_same_factor(pre.GT, gt_or)

@@ -56,6 +56,10 @@ _SIGNATURES = {
     "gbpc_csr_transpose": [_int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp],
     "gbpc_scalarize": [_int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp],
     "gbpc_convert_factor": [_int, _vp, _vp, _vp, _int, _vp, _int, _i32p, _vp],
+    "gbpc_fsai_refit": [_int, _vp, _vp, _vp, _int, _vp, _vp, _int, _dbl, _vp, _int, _i32p, _vp],
+    "gbpc_transpose_map": [_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gbpc_scatter_values": [ctypes.c_int64, _vp, _vp, _vp, _int, _vp],
+    "gbpc_op_fsai_refill": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _vp],
     "gbpc_op_sparse": [_int, _int, _int, _vp, _vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_op_fsai": [_int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp,
                      ctypes.POINTER(_vp)],
@@ -63,6 +67,7 @@ _SIGNATURES = {
     "gbpc_sqlap_rhs": [_vp, _vp, _vp, _vp],
     "gbpc_op_diagonal": [_int, _int, _vp, _vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_op_block_jacobi": [_int, _int, _vp, _vp, _vp, _int, _dbl, _vp, _vp, ctypes.POINTER(_vp)],
+    "gbpc_op_block_jacobi_update": [_vp, _int, _int, _vp, _vp, _vp, _int, _dbl, _vp, _vp],
     "gbpc_op_bilu0": [_int, _int, _vp, _vp, _vp, _int, _int, _int, _dbl, _dbl, _vp, _vp, _vp,
                       ctypes.POINTER(_vp)],
     "gbpc_block_fsai_setup": [_int, _int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp],

@@ -66,12 +66,13 @@ class BlockJacobi(LinearOperator):
             self.shape, self.dtype, self.device,
         ):
             raise ValueError("update requires the same shape, dtype, and device")
-        saved = self.inverse_diagonal
-        try:
-            self._op = self._build(A)
-        except ValueError:
-            self.inverse_diagonal = saved
-            raise
+        # In place (the operator's inverse and inverse_diagonal keep their
+        # storage, so captured applies see the new values); a failed update
+        # changes nothing.
+        _lib.call("gbpc_op_block_jacobi_update", self._op.handle, A.nrow, self.block,
+                  _lib.ptr(A.offsets), _lib.ptr(A.columns), _lib.ptr(A.values),
+                  _lib.dtype_code(A.scalar_type), self.pivot_tolerance,
+                  _lib.ptr(self.inverse_diagonal), _lib.stream(A.device))
         self.A = A
         return self
 

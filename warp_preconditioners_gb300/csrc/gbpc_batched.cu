@@ -195,6 +195,8 @@ bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __
              const V* __restrict__ val, const T* X, const T* Y, T* Z, double alpha, double beta,
              int alpha_zero, int alpha_one, int beta_zero, const T* wm, const T* X2,
              const int* guard, BRed red) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (guard_off(guard)) return;
   constexpr int GR = 32 / KP;
   const int lane = threadIdx.x & 31;
@@ -286,6 +288,8 @@ bdot_kernel(int64_t n, int k, const T* a, const T* b, BRed red) {
 template <typename T, int KP>
 __global__ void __launch_bounds__(kBThreads)
 bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, const T* AP, BRed red) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (*(volatile int*)&bs->any_active == 0) return;
   B_ROWS(KP);
   const bool on = j < k && bs->active[j];
@@ -312,6 +316,8 @@ bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, co
 template <typename T, int KP>
 __global__ void __launch_bounds__(kBThreads)
 bxpay_kernel(int64_t n, int k, const BatchScalars* bs, const T* Zv, T* P) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (*(volatile const int*)&bs->any_active == 0) return;
   B_ROWS(KP);
   if (j >= k || !bs->active[j]) return;
@@ -446,13 +452,15 @@ static void launch_bspmm(const BCsr& m, int k, const void* X, const void* Y, voi
     constexpr int KP = decltype(kpc)::value;
     const int g = b_grid(m.nrow, KP);
     if (dot && dot->w)
-      bspmm_kernel<V, T, EPI, true, KP><<<g, kBThreads, 0, st>>>(
-          m.nrow, k, m.off.as<int32_t>(), m.col.as<int32_t>(), m.val.as<V>(), (const T*)X,
-          (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard, red);
+      launch_k(bspmm_kernel<V, T, EPI, true, KP>, g, kBThreads, 0, st, m.nrow, k,
+               (const int32_t*)m.off.as<int32_t>(), (const int32_t*)m.col.as<int32_t>(),
+               (const V*)m.val.as<V>(), (const T*)X, (const T*)Y, (T*)Z, alpha, beta, az, a1, bz,
+               (const T*)wm, (const T*)X2, guard, red);
     else
-      bspmm_kernel<V, T, EPI, false, KP><<<g, kBThreads, 0, st>>>(
-          m.nrow, k, m.off.as<int32_t>(), m.col.as<int32_t>(), m.val.as<V>(), (const T*)X,
-          (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard, red);
+      launch_k(bspmm_kernel<V, T, EPI, false, KP>, g, kBThreads, 0, st, m.nrow, k,
+               (const int32_t*)m.off.as<int32_t>(), (const int32_t*)m.col.as<int32_t>(),
+               (const V*)m.val.as<V>(), (const T*)X, (const T*)Y, (T*)Z, alpha, beta, az, a1, bz,
+               (const T*)wm, (const T*)X2, guard, red);
   });
 }
 
@@ -613,6 +621,7 @@ struct BSolver {
   std::vector<Cached> graphs;
   uint64_t clock = 0;
   int unroll = 8;
+  bool use_pdl = true;  // programmatic dependent launches inside the loop body
 
   ~BSolver() {
     drop();
@@ -666,15 +675,16 @@ struct BSolver {
     BRed rr = red(R.p, BF_RR);
     with_kp(k, [&](auto kpc) {
       constexpr int KP = decltype(kpc)::value;
-      bcg_update_kernel<T, KP><<<b_grid(n, KP), kBThreads, 0, st>>>(
-          n, k, S(), (T*)X, (T*)R.p, (const T*)P.p, (const T*)AP.p, rr);
+      launch_k(bcg_update_kernel<T, KP>, b_grid(n, KP), kBThreads, 0, st, n, k, S(), (T*)X,
+               (T*)R.p, (const T*)P.p, (const T*)AP.p, rr);
     });
     GBPC_CUDA_TRY(cudaGetLastError());
     BRed rb = red(R.p, BF_BETA);
     if ((rc = M->apply(k, R.p, nullptr, Zv.p, 1.0, 0.0, guard, &rb, st))) return rc;
     with_kp(k, [&](auto kpc) {
       constexpr int KP = decltype(kpc)::value;
-      bxpay_kernel<T, KP><<<b_grid(n, KP), kBThreads, 0, st>>>(n, k, S(), (const T*)Zv.p, (T*)P.p);
+      launch_k(bxpay_kernel<T, KP>, b_grid(n, KP), kBThreads, 0, st, n, k,
+               (const BatchScalars*)S(), (const T*)Zv.p, (T*)P.p);
     });
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
@@ -731,7 +741,10 @@ struct BSolver {
         rc = GBPC_ERR_CUDA;
         break;
       }
-      for (int u = 0; u < unroll && !rc; ++u) rc = record_iteration<T>(k, X, cs);
+      {
+        PdlScope scope(use_pdl);
+        for (int u = 0; u < unroll && !rc; ++u) rc = record_iteration<T>(k, X, cs);
+      }
       e = cudaStreamEndCapture(cs, &g2);
       if (rc) break;
       if (e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
@@ -773,6 +786,10 @@ struct BSolver {
       if (c.b == B && c.x == X && c.k == k) hit = &c;
     if (!hit) {
       rc = (vdtype == GBPC_F64) ? build<double>(k, B, X, st) : build<float>(k, B, X, st);
+      if (rc && use_pdl) {  // capture without programmatic launches instead
+        use_pdl = false;
+        rc = (vdtype == GBPC_F64) ? build<double>(k, B, X, st) : build<float>(k, B, X, st);
+      }
       if (rc) return rc;
       hit = &graphs.back();
     }

@@ -111,6 +111,17 @@ struct Reduction {
   double* out;             // FIN_STORE destination
 };
 
+// Programmatic dependent launch.  Kernels of the Krylov loop body are
+// launched with cudaLaunchAttributeProgrammaticStreamSerialization, so the
+// next kernel is scheduled while this one drains instead of after it; every
+// such kernel first waits (in hardware, no polling) until its predecessor
+// has completed and its writes are visible.  Launched without the attribute,
+// both instructions do nothing.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ bool guard_off(const int* guard) {
   return guard != nullptr && *(volatile const int*)guard == 0;
 }
@@ -217,6 +228,28 @@ __device__ __forceinline__ void reduce_and_finalize(const Reduction& red, double
       finalize(red, total);
     }
   }
+}
+
+// True while a PdlScope is open on this thread (and GBPC_PDL is not "0").
+bool pdl_active();
+
+// Kernel launch that adds the programmatic-serialisation attribute while
+// pdl_active(); the kernel must call pdl_wait() before reading anything its
+// predecessor wrote.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kernel)(KArgs...), int grid, int block, size_t smem,
+                            cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_active() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 inline int grid_for(int64_t items, int per_cta) {

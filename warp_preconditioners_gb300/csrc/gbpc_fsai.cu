@@ -24,6 +24,7 @@
 // SPD input assembled by summation is); other inputs are rejected.
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "gbpc_common.cuh"
@@ -404,6 +405,237 @@ fsai_build_kernel(BuildParams P, const int32_t* __restrict__ off, const int32_t*
 }
 
 // ---------------------------------------------------------------------------
+// The same build for widths <= 16 with lanes = rows: a warp owns 32
+// consecutive rows.  Candidate scoring and selection stay cooperative, one
+// row at a time (every lane on a slice of that row's frontier, as above),
+// but the bordered factorisation, the substitution L^T z = v and the stop
+// tests of all 32 rows then run at once, lane r on row r, with the same
+// operations in the same order as the warp-per-row kernel.  On this GPU an
+// FP64 warp instruction costs the same however many lanes are active; in
+// the warp-per-row kernel those sequential steps ran on one lane and were
+// ~90% of its FP64 instructions.  Rows whose frontier overflows the
+// candidate table are handed to the warp-per-row rerun like there.
+
+constexpr int kLanesWarps = 4;
+
+__host__ __device__ constexpr size_t lanes_smem_bytes(int T_size, int W, int SC, int H) {
+  return ((size_t)T_size * ((size_t)H + 32 * (size_t)W) +
+          sizeof(int) * ((size_t)H + 32 * (size_t)W + 32 * (size_t)SC) + 15) &
+         ~(size_t)15;
+}
+
+template <typename T, int WMAX>
+__global__ void __launch_bounds__(32 * kLanesWarps)
+fsai_build_lanes_kernel(BuildParams P, const int32_t* __restrict__ off,
+                        const int32_t* __restrict__ col, const T* __restrict__ ahat,
+                        const T* __restrict__ ahatT, const T* __restrict__ scale, T tolerance,
+                        T pivot_floor, int32_t* ell_cols, T* ell_vals, int32_t* row_counts,
+                        int32_t* status) {
+  extern __shared__ __align__(16) unsigned char lanes_smem[];
+  using BitsT = Bits<T>;
+  using U = typename BitsT::U;
+  const int W = P.width, H = P.hsize;
+  const int SC = min(P.step, W);  // candidates ever used per round
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row0 = ((int64_t)blockIdx.x * kLanesWarps + warp) * 32;
+  if (row0 >= P.n) return;
+  unsigned char* base = lanes_smem + (size_t)warp * lanes_smem_bytes((int)sizeof(T), W, SC, H);
+  T* hacc = reinterpret_cast<T*>(base);  // [H]
+  T* zS = hacc + H;                      // [32][W]
+  int* hkey = reinterpret_cast<int*>(zS + 32 * W);  // [H]
+  int* patS = hkey + H;                  // [32][W]
+  int* candS = patS + 32 * W;            // [32][SC]
+  const int hmask = H - 1;
+  const int i = (int)row0 + lane;
+  const bool exists = i < P.n;
+  T* z = zS + lane * W;
+  int* pat = patS + lane * W;
+  // Packed lower triangle by columns, as in the warp-per-row kernel.
+  T Lp[WMAX * (WMAX + 1) / 2];
+  T v[WMAX], a[WMAX], wv[WMAX];
+  auto L = [&](int r, int p) -> T& { return Lp[p * W - (p * (p - 1)) / 2 + (r - p)]; };
+  int size = 1, nsel = 0;
+  bool active = exists, stopped = false, truncated = false, overflowed = false;
+  if (exists) {
+    pat[0] = i;
+    z[0] = T(1);
+    L(0, 0) = T(1);
+    v[0] = T(1);
+  }
+  __syncwarp();
+  while (true) {
+    const bool grow = active && !overflowed && size < W;
+    const unsigned mask = __ballot_sync(0xffffffffu, grow);
+    if (mask == 0u) break;
+    // Scoring and selection, one growing row at a time.
+    for (int r = 0; r < 32; ++r) {
+      if (!((mask >> r) & 1u)) continue;
+      const int rsize = __shfl_sync(0xffffffffu, size, r);
+      const int ri = (int)row0 + r;
+      const int* rpat = patS + r * W;
+      const T* rz = zS + r * W;
+      for (int s2 = lane; s2 < H; s2 += 32) {
+        hkey[s2] = kEmpty;
+        hacc[s2] = T(0);
+      }
+      __syncwarp();
+      bool overflow = false;
+      for (int q = 0; q < rsize; ++q) {
+        const int pq = rpat[q];
+        const T zq = rz[q];
+        const int e_end = off[pq + 1];
+        for (int e = off[pq] + lane; e < e_end; e += 32) {
+          const int c = col[e];
+          if (c >= ri) continue;
+          bool member = false;
+          for (int t = 0; t < rsize; ++t) member |= (rpat[t] == c);
+          if (member) continue;
+          const int slot = hfind_insert(hkey, hmask, P.hbits, c);
+          if (slot < 0) {
+            overflow = true;
+          } else {
+            const T t = ahatT[e] * zq;
+            hacc[slot] = hacc[slot] + t;
+          }
+        }
+        __syncwarp();
+      }
+      if (__any_sync(0xffffffffu, overflow)) {
+        if (lane == r) overflowed = true;
+        continue;
+      }
+      // Top candidates: higher score, then lower column (as above).
+      const int want = min(SC, W - rsize);
+      int ns = 0;
+      for (int k = 0; k < want; ++k) {
+        U best_bits = 0;
+        int best_col = 0x7fffffff;
+        int best_slot = -1;
+        for (int s2 = lane; s2 < H; s2 += 32) {
+          const int kk = hkey[s2];
+          if (kk < 0) continue;
+          const U bits = BitsT::abs_bits(hacc[s2]);
+          if (bits == 0 || bits > BitsT::kInf) continue;
+          if (bits > best_bits || (bits == best_bits && kk < best_col)) {
+            best_bits = bits;
+            best_col = kk;
+            best_slot = s2;
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const U ob = __shfl_xor_sync(0xffffffffu, best_bits, o);
+          const int oc = __shfl_xor_sync(0xffffffffu, best_col, o);
+          const int os = __shfl_xor_sync(0xffffffffu, best_slot, o);
+          if (ob > best_bits || (ob == best_bits && oc < best_col)) {
+            best_bits = ob;
+            best_col = oc;
+            best_slot = os;
+          }
+        }
+        if (best_slot < 0) break;
+        if (lane == 0) {
+          candS[r * SC + k] = best_col;
+          hkey[best_slot] = kTomb;
+        }
+        __syncwarp();
+        ++ns;
+      }
+      if (lane == r) nsel = ns;
+    }
+    __syncwarp();
+    // Factor updates of every growing row at once.
+    if (grow && !overflowed) {
+      if (nsel == 0) {
+        active = false;
+      } else {
+        const T old_z0 = z[0];
+        for (int k = 0; k < nsel; ++k) {
+          if (size == W) break;
+          const int best = candS[lane * SC + k];
+          const int b0 = off[best], b1 = off[best + 1];
+          for (int p = 0; p < size; ++p) {
+            const int pc = pat[p];
+            const int lo = lower_bound_row(col, b0, b1, pc);
+            a[p] = (lo < b1 && col[lo] == pc) ? ahat[lo] : T(0);
+          }
+          T pivot = T(1);
+          T rhs = T(0);
+          for (int p = 0; p < size; ++p) {
+            const T wp = a[p] / L(p, p);
+            wv[p] = wp;
+            const T sq = wp * wp;
+            pivot = pivot - sq;
+            const T pr = wp * v[p];
+            rhs = rhs - pr;
+            for (int l = p + 1; l < size; ++l) {
+              const T t = L(l, p) * wp;
+              a[l] = a[l] - t;
+            }
+          }
+          if (pivot <= pivot_floor || !isfinite(pivot)) {
+            truncated = true;
+            stopped = true;
+            break;
+          }
+          for (int p = 0; p < size; ++p) L(size, p) = wv[p];
+          pat[size] = best;
+          const T d = sqrt(pivot);
+          L(size, size) = d;
+          v[size] = rhs / d;
+          ++size;
+        }
+        // L^T z = v, in the reference's order.
+        for (int p = size - 1; p >= 0; --p) {
+          T acc = v[p];
+          for (int q = p + 1; q < size; ++q) {
+            const T t = L(q, p) * z[q];
+            acc = acc - t;
+          }
+          z[p] = acc / L(p, p);
+        }
+        if (stopped) {
+          active = false;
+        } else if (tolerance > T(0)) {
+          const T ratio = old_z0 / z[0];
+          if (T(1) - ratio <= tolerance) active = false;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (!exists) return;
+  if (overflowed) {
+    const int k = atomicAdd(P.overflow_count, 1);
+    P.overflow_list[k] = i;
+    return;
+  }
+  // Normalise, validate, sort by column, write the ELL row.
+  const T norm = sqrt(z[0]);
+  bool valid = true;
+  int32_t* oc = ell_cols + (size_t)i * W;
+  T* ov = ell_vals + (size_t)i * W;
+  for (int p = 0; p < size; ++p) {
+    const int c = pat[p];
+    const T t = z[p] / norm;
+    const T val = t * scale[c];
+    if (!isfinite(val)) valid = false;
+    if (p == 0 && !(val > T(0))) valid = false;
+    int rank = 0;
+    for (int q = 0; q < size; ++q) rank += (pat[q] < c);
+    oc[rank] = c;
+    ov[rank] = val;
+  }
+  for (int p = size; p < W; ++p) {
+    oc[p] = -1;
+    ov[p] = T(0);
+  }
+  row_counts[i] = size;
+  if (truncated) atomicAdd(status + 1, 1);
+  if (!valid) atomicAdd(status + 2, 1);
+}
+
+// ---------------------------------------------------------------------------
 // Scans, packing, transpose, scalarise, conversion.
 
 // Exclusive scan of int32 counts into out[0..n] (out[n] = total), 1024 per CTA.
@@ -562,10 +794,234 @@ __global__ void convert_factor_kernel(int n, const int32_t* __restrict__ off,
   if (bad) atomicAdd(invalid, 1);
 }
 
+// ---------------------------------------------------------------------------
+// Fixed-support numeric refit (fsai_reuse.py:75-149, kernel `refit`), one
+// warp per row.
+//
+// Row i keeps its support S (the sorted columns of G's row i, diagonal
+// last).  The scaled local matrix A_S = diag(s) A[S,S] diag(s) is factored
+// A_S = L L^T, z = A_S^-1 e_i by a forward and a backward substitution, and
+// g_i[S] = z / sqrt(z_i) * s[S].  Every value is formed with the reference's
+// operations in the reference's order: the right-looking factorisation
+// applies the subtractions of each element in the same k order as the
+// reference's row-by-row loop, the forward substitution runs column by
+// column across lanes in the same order, and the backward substitution runs
+// on one lane because its sums run in increasing column order.  With
+// contraction disabled the factor is bit-identical to a sequential
+// evaluation of the reference loop.  Pivots <= floor or non-finite are
+// replaced by 1 and the row is counted invalid, as in the reference.
+
+constexpr int kRefitWarps = 4;
+
+__device__ __forceinline__ int tri_index(int p, int q) { return p * (p + 1) / 2 + q; }
+
+// (p, q), q <= p, of lower-triangle index t (row-major).
+__device__ __forceinline__ void tri_decode(int t, int& p, int& q) {
+  p = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (p > 0 && tri_index(p, 0) > t) --p;
+  while (tri_index(p + 1, 0) <= t) ++p;
+  q = t - tri_index(p, 0);
+}
+
+__device__ __forceinline__ bool finite_value(double v) { return isfinite(v); }
+__device__ __forceinline__ bool finite_value(float v) { return isfinite(v); }
+__device__ __forceinline__ bool finite_value(__nv_bfloat16 v) { return isfinite(__bfloat162float(v)); }
+__device__ __forceinline__ bool nonpositive(double v) { return v <= 0.0; }
+__device__ __forceinline__ bool nonpositive(float v) { return v <= 0.0f; }
+__device__ __forceinline__ bool nonpositive(__nv_bfloat16 v) { return __bfloat162float(v) <= 0.0f; }
+
+template <typename T, typename S>
+__global__ void __launch_bounds__(32 * kRefitWarps)
+fsai_refit_kernel(int n, const int32_t* __restrict__ a_off, const int32_t* __restrict__ a_col,
+                  const T* __restrict__ a_val, const T* __restrict__ scale,
+                  const int32_t* __restrict__ g_off, const int32_t* __restrict__ g_col, int width,
+                  T floor, S* out, int32_t* bad) {
+  extern __shared__ __align__(16) unsigned char refit_smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int row = blockIdx.x * kRefitWarps + w;
+  const int tri_len = tri_index(width, 0);
+  T* tri = reinterpret_cast<T*>(refit_smem) + (size_t)w * (tri_len + width);
+  T* z = tri + tri_len;
+  if (row >= n) return;
+  const int start = g_off[row];
+  const int s = g_off[row + 1] - start;
+  if (s < 1 || s > width) {
+    if (lane == 0) atomicAdd(bad, 1);
+    return;
+  }
+  // Scaled local matrix, lower triangle: (a_rc * s_r) * s_c.
+  for (int t = lane; t < tri_index(s, 0); t += 32) {
+    int p, q;
+    tri_decode(t, p, q);
+    const int r = g_col[start + p], c = g_col[start + q];
+    const int lo = lower_bound_row(a_col, a_off[r], a_off[r + 1], c);
+    T a = T(0);
+    if (lo < a_off[r + 1] && a_col[lo] == c) a = a_val[lo] * scale[r] * scale[c];
+    tri[t] = a;
+  }
+  __syncwarp();
+  bool valid = true;
+  for (int k = 0; k < s; ++k) {
+    T d = tri[tri_index(k, k)];
+    if (d <= floor || !isfinite(d)) {
+      valid = false;
+      d = T(1);
+    }
+    const T ckk = sqrt(d);
+    __syncwarp();
+    if (lane == 0) tri[tri_index(k, k)] = ckk;
+    for (int p = k + 1 + lane; p < s; p += 32) tri[tri_index(p, k)] = tri[tri_index(p, k)] / ckk;
+    __syncwarp();
+    const int m = s - k - 1;
+    for (int t = lane; t < tri_index(m, 0); t += 32) {
+      int pp, qq;
+      tri_decode(t, pp, qq);
+      const int p = k + 1 + pp, q = k + 1 + qq;
+      tri[tri_index(p, q)] = tri[tri_index(p, q)] - tri[tri_index(p, k)] * tri[tri_index(q, k)];
+    }
+    __syncwarp();
+  }
+  // Forward substitution L y = e_i, column by column (rows lane, lane + 32).
+  T a0 = (lane < s && g_col[start + lane] == row) ? T(1) : T(0);
+  T a1 = (lane + 32 < s && g_col[start + lane + 32] == row) ? T(1) : T(0);
+  for (int q = 0; q < s; ++q) {
+    if (q == lane) z[q] = a0 / tri[tri_index(q, q)];
+    if (q == lane + 32) z[q] = a1 / tri[tri_index(q, q)];
+    __syncwarp();
+    const T zq = z[q];
+    if (lane > q && lane < s) a0 = a0 - tri[tri_index(lane, q)] * zq;
+    if (lane + 32 > q && lane + 32 < s) a1 = a1 - tri[tri_index(lane + 32, q)] * zq;
+  }
+  __syncwarp();
+  // Backward substitution L^T z = y, one lane (sums in increasing q).
+  if (lane == 0) {
+    for (int p = s - 1; p >= 0; --p) {
+      T a = z[p];
+      for (int q = p + 1; q < s; ++q) a = a - tri[tri_index(q, p)] * z[q];
+      z[p] = a / tri[tri_index(p, p)];
+    }
+  }
+  __syncwarp();
+  const T norm = sqrt(z[s - 1]);
+  bool ok = true;
+  for (int p = lane; p < s; p += 32) {
+    const S v = narrow<T, S>(z[p] / norm * scale[g_col[start + p]]);
+    out[start + p] = v;
+    if (!finite_value(v)) ok = false;
+    if (p == s - 1 && nonpositive(v)) ok = false;
+  }
+  ok = __all_sync(0xffffffffu, ok) && valid;
+  if (lane == 0 && !ok) atomicAdd(bad, 1);
+}
+
+// The same refit with one thread per row, for supports of at most W entries:
+// the reference's loop itself (fsai_reuse.py:97-149), so every lane issues
+// useful FP64 work.  On this GPU an FP64 warp instruction costs the same
+// however many lanes are active, which makes the warp-per-row version's
+// one-lane steps (substitutions, divisions) its bottleneck for small
+// supports; wider supports stay with it, because per-thread arrays of
+// W(W+1)/2 words would need a large local-memory reservation.
+template <typename T, typename S, int W>
+__global__ void __launch_bounds__(128)
+fsai_refit_row_kernel(int n, const int32_t* __restrict__ a_off, const int32_t* __restrict__ a_col,
+                      const T* __restrict__ a_val, const T* __restrict__ scale,
+                      const int32_t* __restrict__ g_off, const int32_t* __restrict__ g_col,
+                      T floor, S* out, int32_t* bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int start = g_off[i];
+  const int size = g_off[i + 1] - start;
+  if (size < 1 || size > W) {
+    atomicAdd(bad, 1);
+    return;
+  }
+  T chol[W * (W + 1) / 2];
+  T z[W];
+  bool valid = true;
+  for (int p = 0; p < size; ++p) {
+    const int r = g_col[start + p];
+    const int rlo = a_off[r], rhi = a_off[r + 1];
+    for (int q = 0; q <= p; ++q) {
+      const int c = g_col[start + q];
+      const int lo = lower_bound_row(a_col, rlo, rhi, c);
+      T a = T(0);
+      if (lo < rhi && a_col[lo] == c) a = a_val[lo] * scale[r] * scale[c];
+      for (int k = 0; k < q; ++k) a = a - chol[tri_index(p, k)] * chol[tri_index(q, k)];
+      if (p == q) {
+        if (a <= floor || !isfinite(a)) {
+          valid = false;
+          a = T(1);
+        }
+        chol[tri_index(p, p)] = sqrt(a);
+      } else {
+        chol[tri_index(p, q)] = a / chol[tri_index(q, q)];
+      }
+    }
+  }
+  for (int p = 0; p < size; ++p) {
+    T a = (g_col[start + p] == i) ? T(1) : T(0);
+    for (int q = 0; q < p; ++q) a = a - chol[tri_index(p, q)] * z[q];
+    z[p] = a / chol[tri_index(p, p)];
+  }
+  for (int p = size - 1; p >= 0; --p) {
+    T a = z[p];
+    for (int q = p + 1; q < size; ++q) a = a - chol[tri_index(q, p)] * z[q];
+    z[p] = a / chol[tri_index(p, p)];
+  }
+  const T norm = sqrt(z[size - 1]);
+  for (int p = 0; p < size; ++p) {
+    const S v = narrow<T, S>(z[p] / norm * scale[g_col[start + p]]);
+    out[start + p] = v;
+    if (!finite_value(v)) valid = false;
+    if (p == size - 1 && nonpositive(v)) valid = false;
+  }
+  if (!valid) atomicAdd(bad, 1);
+}
+
+// map[e] = position of entry (i, j) of a CSR matrix in its transpose's row j.
+__global__ void transpose_map_kernel(int nrow, const int32_t* __restrict__ off,
+                                     const int32_t* __restrict__ col,
+                                     const int32_t* __restrict__ t_off,
+                                     const int32_t* __restrict__ t_col, int32_t* map,
+                                     int32_t* missing) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrow) return;
+  for (int e = off[i]; e < off[i + 1]; ++e) {
+    const int j = col[e];
+    const int pos = lower_bound_row(t_col, t_off[j], t_off[j + 1], i);
+    if (pos < t_off[j + 1] && t_col[pos] == i) {
+      map[e] = pos;
+    } else {
+      map[e] = -1;
+      atomicAdd(missing, 1);
+    }
+  }
+}
+
+template <typename V>
+__global__ void scatter_values_kernel(int64_t count, const V* __restrict__ src,
+                                      const int32_t* __restrict__ map, V* dst) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t m = map[e];
+    if (m >= 0) dst[m] = src[e];
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // Host entry points.
+
+// GBPC_FSAI_LANES=0 selects the warp-per-row build for every width (the two
+// builds give identical factors; the switch exists to compare them).
+static bool lanes_build_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBPC_FSAI_LANES");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 template <typename T>
 static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* val, int W,
@@ -648,7 +1104,40 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
   };
-  if ((rc = launch(Hfirst, hbits_first, nullptr, n))) return rc;
+  // First pass: lanes = rows for widths <= 16 (see fsai_build_lanes_kernel).
+  auto launch_lanes = [&](int H, int hbits) -> int {
+    const int SC = std::min(S, W);
+    const size_t per_warp = lanes_smem_bytes((int)sizeof(T), W, SC, H);
+    const size_t smem = per_warp * kLanesWarps;
+    if (smem > (size_t)smem_optin) return launch(H, hbits, nullptr, n);
+    auto kern = (W <= 8) ? fsai_build_lanes_kernel<T, 8> : fsai_build_lanes_kernel<T, 16>;
+    GBPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    BuildParams P;
+    P.n = n;
+    P.width = W;
+    P.step = S;
+    P.hsize = H;
+    P.hbits = hbits;
+    P.psize = PH;
+    P.pbits = pbits;
+    P.rows = nullptr;
+    P.nrows_list = 0;
+    P.overflow_list = ovl.as<int32_t>();
+    P.overflow_count = stat + 5;
+    const int64_t warps_needed = ((int64_t)n + 31) / 32;
+    if (n > 0)
+      kern<<<(int)((warps_needed + kLanesWarps - 1) / kLanesWarps), 32 * kLanesWarps, smem, st>>>(
+          P, off, col, ahat.as<T>(), ahatT.as<T>(), scale, (T)kap, (T)floor_, ell_cols, ell_vals,
+          counts, stat);
+    GBPC_CUDA_TRY(cudaGetLastError());
+    return GBPC_OK;
+  };
+  if (W <= 16 && lanes_build_enabled()) {
+    if ((rc = launch_lanes(Hfirst, hbits_first))) return rc;
+  } else if ((rc = launch(Hfirst, hbits_first, nullptr, n))) {
+    return rc;
+  }
   GBPC_CUDA_TRY(cudaMemcpyAsync(h, stat, sizeof(h), cudaMemcpyDeviceToHost, st));
   GBPC_CUDA_TRY(cudaStreamSynchronize(st));
   if (h[5] > 0) {
@@ -871,5 +1360,128 @@ extern "C" int gbpc_convert_factor(int n, const int32_t* offsets, const int32_t*
     gbpc_set_error("factor_dtype conversion lost finite entries or a positive diagonal");
     return GBPC_ERR_CONVERSION;
   }
+  return GBPC_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Fixed-support refit entry points (fsai_reuse.py:157-245).
+
+namespace gbpc {
+template <typename T, typename S>
+static int refit_t(int n, const int32_t* a_off, const int32_t* a_col, const T* a_val,
+                   const int32_t* g_off, const int32_t* g_col, int width, double floor_, S* out,
+                   int32_t* status_host, cudaStream_t st) {
+  DevBuf scale, status;
+  int rc;
+  if ((rc = scale.alloc(sizeof(T) * std::max(n, 1)))) return rc;
+  if ((rc = status.alloc(sizeof(int32_t) * 2))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int32_t) * 2, st));
+  int32_t* stat = status.as<int32_t>();
+  if (n > 0) {
+    fsai_diag_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, a_off, a_col, a_val, scale.as<T>(),
+                                                          stat);
+    if (width <= 8) {
+      fsai_refit_row_kernel<T, S, 8><<<grid_for(n, 128), 128, 0, st>>>(
+          n, a_off, a_col, a_val, scale.as<T>(), g_off, g_col, (T)floor_, out, stat + 1);
+    } else if (width <= 16) {
+      fsai_refit_row_kernel<T, S, 16><<<grid_for(n, 128), 128, 0, st>>>(
+          n, a_off, a_col, a_val, scale.as<T>(), g_off, g_col, (T)floor_, out, stat + 1);
+    } else {
+      const size_t smem = sizeof(T) * (size_t)(width * (width + 1) / 2 + width) * kRefitWarps;
+      GBPC_CUDA_TRY(cudaFuncSetAttribute(fsai_refit_kernel<T, S>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      fsai_refit_kernel<T, S><<<(n + kRefitWarps - 1) / kRefitWarps, 32 * kRefitWarps, smem,
+                                st>>>(n, a_off, a_col, a_val, scale.as<T>(), g_off, g_col, width,
+                                      (T)floor_, out, stat + 1);
+    }
+  }
+  GBPC_CUDA_TRY(cudaGetLastError());
+  GBPC_CUDA_TRY(cudaMemcpyAsync(status_host, stat, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  return GBPC_OK;
+}
+}  // namespace gbpc
+
+extern "C" int gbpc_fsai_refit(int n, const int32_t* a_off, const int32_t* a_col,
+                               const void* a_val, int dtype, const int32_t* g_off,
+                               const int32_t* g_col, int width, double pivot_floor, void* out,
+                               int factor_dtype, int32_t* status_host, void* stream) {
+  if (n < 0 || width < 1 || width > 64 || !status_host ||
+      (n > 0 && (!a_off || !a_col || !a_val || !g_off || !g_col || !out)) ||
+      !(pivot_floor > 0.0 && pivot_floor < 1.0)) {
+    gbpc_set_error("gbpc_fsai_refit: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GBPC_F64) {
+    if (factor_dtype == GBPC_F64)
+      return refit_t<double, double>(n, a_off, a_col, (const double*)a_val, g_off, g_col, width,
+                                     pivot_floor, (double*)out, status_host, st);
+    if (factor_dtype == GBPC_F32)
+      return refit_t<double, float>(n, a_off, a_col, (const double*)a_val, g_off, g_col, width,
+                                    pivot_floor, (float*)out, status_host, st);
+    if (factor_dtype == GBPC_BF16)
+      return refit_t<double, __nv_bfloat16>(n, a_off, a_col, (const double*)a_val, g_off, g_col,
+                                            width, pivot_floor, (__nv_bfloat16*)out, status_host,
+                                            st);
+  } else if (dtype == GBPC_F32) {
+    if (factor_dtype == GBPC_F32)
+      return refit_t<float, float>(n, a_off, a_col, (const float*)a_val, g_off, g_col, width,
+                                   pivot_floor, (float*)out, status_host, st);
+    if (factor_dtype == GBPC_BF16)
+      return refit_t<float, __nv_bfloat16>(n, a_off, a_col, (const float*)a_val, g_off, g_col,
+                                           width, pivot_floor, (__nv_bfloat16*)out, status_host,
+                                           st);
+  }
+  gbpc_set_error("gbpc_fsai_refit: unsupported matrix / factor dtype pair (%d, %d)", dtype,
+                 factor_dtype);
+  return GBPC_ERR_ARG;
+}
+
+extern "C" int gbpc_transpose_map(int nrow, const int32_t* offsets, const int32_t* columns,
+                                  const int32_t* t_offsets, const int32_t* t_columns,
+                                  int32_t* map_out, void* stream) {
+  if (nrow < 0 || (nrow > 0 && (!offsets || !columns || !t_offsets || !t_columns || !map_out))) {
+    gbpc_set_error("gbpc_transpose_map: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf missing;
+  int rc = missing.alloc(sizeof(int32_t));
+  if (rc) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(missing.p, 0, sizeof(int32_t), st));
+  if (nrow > 0)
+    transpose_map_kernel<<<grid_for(nrow, 256), 256, 0, st>>>(nrow, offsets, columns, t_offsets,
+                                                              t_columns, map_out,
+                                                              missing.as<int32_t>());
+  GBPC_CUDA_TRY(cudaGetLastError());
+  int32_t h = 0;
+  GBPC_CUDA_TRY(cudaMemcpyAsync(&h, missing.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h) {
+    gbpc_set_error("gbpc_transpose_map: %d entries have no transposed counterpart", h);
+    return GBPC_ERR_ARG;
+  }
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_scatter_values(int64_t count, const void* src, const int32_t* map, void* dst,
+                                   int dtype, void* stream) {
+  if (count < 0 || (count > 0 && (!src || !map || !dst)) || !valid_value_dtype(dtype)) {
+    gbpc_set_error("gbpc_scatter_values: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  if (count == 0) return GBPC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int g = (int)std::min<int64_t>((count + 255) / 256, 152 * 8);
+  if (dtype == GBPC_F64)
+    scatter_values_kernel<double><<<g, 256, 0, st>>>(count, (const double*)src, map, (double*)dst);
+  else if (dtype == GBPC_F32)
+    scatter_values_kernel<float><<<g, 256, 0, st>>>(count, (const float*)src, map, (float*)dst);
+  else
+    scatter_values_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(count, (const __nv_bfloat16*)src, map,
+                                                            (__nv_bfloat16*)dst);
+  GBPC_CUDA_TRY(cudaGetLastError());
   return GBPC_OK;
 }

@@ -32,6 +32,16 @@ struct ByteTally {
   ByteTally& operator=(const ByteTally&) = delete;
 };
 
+// While open, kernels launched through launch_k on this thread carry the
+// programmatic dependent launch attribute (gbpc_common.cuh).
+struct PdlScope {
+  bool prev;
+  explicit PdlScope(bool on);
+  ~PdlScope();
+  PdlScope(const PdlScope&) = delete;
+  PdlScope& operator=(const PdlScope&) = delete;
+};
+
 // Owned device allocation.
 struct DevBuf {
   void* p = nullptr;
@@ -82,6 +92,9 @@ struct SellBuild {
   const void* row_scale = nullptr;  // optional per-source-row factor (input value dtype)
 };
 
+// Rewrites the values of a Sell built from the same pattern (off, col, opt).
+int sell_refill(Sell& s, const int32_t* off, const int32_t* col, const void* val, int in_dtype,
+                const SellBuild& opt, cudaStream_t st);
 int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,
                const void* val, int in_dtype, int out_dtype, const SellBuild& opt,
                cudaStream_t st);

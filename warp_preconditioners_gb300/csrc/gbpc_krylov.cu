@@ -39,6 +39,8 @@ __device__ __forceinline__ bool inactive(const KrylovScalars* ks) {
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const double* p,
                  const double* Ap, Reduction red) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (inactive(ks)) return;
   const double alpha = ks->alpha;
   double part = 0.0;
@@ -56,6 +58,8 @@ cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const doubl
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, const double* p,
                  const double* Ap, const double* y, Reduction red) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (inactive(ks)) return;
   const double alpha = ks->alpha;
   double part = 0.0;
@@ -74,6 +78,8 @@ cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, 
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, const double* w,
             double* q) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (inactive(ks)) return;
   const double beta = ks->beta;
   for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
@@ -122,6 +128,7 @@ struct Solver {
   int64_t n = 0;
   bool use_graph = true;
   int unroll = 8;  // iterations per pass of the device loop (measured: 1 -> 8 saves ~4 us/iteration)
+  bool use_pdl = true;  // programmatic dependent launches inside the loop body
   DevBuf r, z, p, Ap, Az, y, ks, zeros;
   ReduceBuf rb;
   // Cached graph for the last (b, x) pair.
@@ -210,24 +217,25 @@ struct Solver {
     if (method == GBPC_CG) {
       DotSpec da = dot(p.as<double>(), FIN_CG_ALPHA);
       if ((rc = A->apply(p.p, nullptr, Ap.p, 1.0, 0.0, guard, &da, st))) return rc;
-      cg_update_kernel<<<vec_grid(n), kThreads, 0, st>>>(n, K(), x, r.as<double>(), p.as<double>(),
-                                                         Ap.as<double>(), rrr);
-      GBPC_CUDA_TRY(cudaGetLastError());
+      GBPC_CUDA_TRY(launch_k(cg_update_kernel, vec_grid(n), kThreads, 0, st, n, K(), x,
+                             r.as<double>(), (const double*)p.as<double>(),
+                             (const double*)Ap.as<double>(), rrr));
       DotSpec db = dot(r.as<double>(), FIN_CG_BETA);
       if ((rc = precondition(r.as<double>(), z.as<double>(), guard, &db, st))) return rc;
-      xpay_kernel<<<vec_grid(n), kThreads, 0, st>>>(n, K(), z.as<double>(), p.as<double>(), nullptr,
-                                                    nullptr);
+      GBPC_CUDA_TRY(launch_k(xpay_kernel, vec_grid(n), kThreads, 0, st, n,
+                             (const KrylovScalars*)K(), (const double*)z.as<double>(),
+                             p.as<double>(), (const double*)nullptr, (double*)nullptr));
     } else {
       DotSpec da = dot(Ap.as<double>(), FIN_CR_ALPHA);
       if ((rc = precondition(Ap.as<double>(), y.as<double>(), guard, &da, st))) return rc;
-      cr_update_kernel<<<vec_grid(n), kThreads, 0, st>>>(n, K(), x, r.as<double>(), z.as<double>(),
-                                                         p.as<double>(), Ap.as<double>(),
-                                                         y.as<double>(), rrr);
-      GBPC_CUDA_TRY(cudaGetLastError());
+      GBPC_CUDA_TRY(launch_k(cr_update_kernel, vec_grid(n), kThreads, 0, st, n, K(), x,
+                             r.as<double>(), z.as<double>(), (const double*)p.as<double>(),
+                             (const double*)Ap.as<double>(), (const double*)y.as<double>(), rrr));
       DotSpec db = dot(z.as<double>(), FIN_CG_BETA);
       if ((rc = A->apply(z.p, nullptr, Az.p, 1.0, 0.0, guard, &db, st))) return rc;
-      xpay_kernel<<<vec_grid(n), kThreads, 0, st>>>(n, K(), z.as<double>(), p.as<double>(),
-                                                    Az.as<double>(), Ap.as<double>());
+      GBPC_CUDA_TRY(launch_k(xpay_kernel, vec_grid(n), kThreads, 0, st, n,
+                             (const KrylovScalars*)K(), (const double*)z.as<double>(),
+                             p.as<double>(), (const double*)Az.as<double>(), Ap.as<double>()));
     }
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
@@ -289,7 +297,10 @@ struct Solver {
       // `unroll` guarded iterations per pass of the while-node: the loop
       // condition is evaluated once per pass, and iterations after
       // convergence inside a pass return immediately from every kernel.
-      for (int u = 0; u < unroll && !rc; ++u) rc = record_iteration(x, cs);
+      {
+        PdlScope scope(use_pdl);
+        for (int u = 0; u < unroll && !rc; ++u) rc = record_iteration(x, cs);
+      }
       e = cudaStreamEndCapture(cs, &g2);
       if (rc) break;
       if (e != cudaSuccess) {
@@ -321,7 +332,12 @@ struct Solver {
     int rc;
     if (use_graph) {
       if (!exec || last_b != b || last_x != x) {
-        if ((rc = build_graph(b, x, st))) return rc;
+        rc = build_graph(b, x, st);
+        if (rc && use_pdl) {  // capture without programmatic launches instead
+          use_pdl = false;
+          rc = build_graph(b, x, st);
+        }
+        if (rc) return rc;
       }
       set_scalars_kernel<<<1, 1, 0, st>>>(K(), tol, atol, maxiter, (unsigned long long)handle);
       GBPC_CUDA_TRY(cudaGetLastError());

@@ -400,6 +400,22 @@ extern "C" int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int
   return GBPC_OK;
 }
 
+extern "C" int gbpc_op_fsai_refill(gbpc_op* h, const int32_t* g_off, const int32_t* g_col,
+                                   const void* g_val, const int32_t* gt_off,
+                                   const int32_t* gt_col, const void* gt_val, int value_dtype,
+                                   void* stream) {
+  auto* op = h ? dynamic_cast<FsaiOp*>(h->impl.get()) : nullptr;
+  if (!op || !g_off || !gt_off || !valid_value_dtype(value_dtype)) {
+    gbpc_set_error("gbpc_op_fsai_refill: needs an FSAI operator and its factor arrays");
+    return GBPC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int in = input_dtype(value_dtype);
+  int rc = sell_refill(op->g, g_off, g_col, g_val, in, SellBuild{}, st);
+  if (!rc) rc = sell_refill(op->gt, gt_off, gt_col, gt_val, in, SellBuild{}, st);
+  return rc;
+}
+
 extern "C" int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* columns,
                              const void* values, int dtype, const void* mass,
                              const int32_t* free_indices, int nfree, double mass_weight,
@@ -600,6 +616,42 @@ extern "C" int gbpc_op_block_jacobi(int nrow, int block, const int32_t* offsets,
     return rc;
   }
   GBPC_OUT_OP(op);
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_op_block_jacobi_update(gbpc_op* h, int nrow, int block,
+                                           const int32_t* offsets, const int32_t* columns,
+                                           const void* values, int dtype, double pivot_tolerance,
+                                           void* inverse_out, void* stream) {
+  auto* op = h ? dynamic_cast<BlockJacobiOp*>(h->impl.get()) : nullptr;
+  if (!op || nrow != op->nrow || block != op->B || dtype != op->vdtype) {
+    gbpc_set_error("gbpc_op_block_jacobi_update: needs a BlockJacobi operator of the same "
+                   "shape and dtype");
+    return GBPC_ERR_ARG;
+  }
+  if (!std::isfinite(pivot_tolerance) || pivot_tolerance < 0) {
+    gbpc_set_error("pivot_tolerance must be finite and nonnegative");
+    return GBPC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = dtype_size(dtype) * (size_t)nrow * block * block;
+  DevBuf cand;
+  int rc = cand.alloc(std::max<size_t>(bytes, 16));
+  if (rc) return rc;
+  int32_t bad = 0;
+  rc = block_diag_inverse(nrow, block, offsets, columns, values, dtype, pivot_tolerance, cand.p,
+                          &bad, st);
+  if (rc) return rc;
+  if (bad) {  // the previous inverse stays in place
+    gbpc_set_error("Missing, nonfinite or singular/near-singular block pivot");
+    return GBPC_ERR_PIVOT;
+  }
+  if (bytes) {
+    GBPC_CUDA_TRY(cudaMemcpyAsync(op->inv.p, cand.p, bytes, cudaMemcpyDeviceToDevice, st));
+    if (inverse_out)
+      GBPC_CUDA_TRY(cudaMemcpyAsync(inverse_out, cand.p, bytes, cudaMemcpyDeviceToDevice, st));
+  }
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
   return GBPC_OK;
 }
 

@@ -7,6 +7,7 @@
 // sum uses two interleaved accumulators to halve the dependent-FMA chain.
 
 #include <atomic>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
@@ -65,7 +66,18 @@ bool valid_value_dtype(int d) { return d == GBPC_F64 || d == GBPC_F32 || d == GB
 namespace {
 std::atomic<size_t> g_live_bytes{0};
 thread_local size_t* t_tally = nullptr;
+thread_local bool t_pdl = false;
 }  // namespace
+
+bool pdl_active() {
+  static const bool enabled = [] {
+    const char* e = std::getenv("GBPC_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return t_pdl && enabled;
+}
+PdlScope::PdlScope(bool on) : prev(t_pdl) { t_pdl = on; }
+PdlScope::~PdlScope() { t_pdl = prev; }
 
 size_t* current_tally() { return t_tally; }
 size_t device_bytes_live() { return g_live_bytes.load(); }
@@ -238,6 +250,7 @@ __global__ void sell_fill_kernel(int nrow, int nslices, int B, const int32_t* __
         c = colmap[c];
         if (c < 0) continue;
       }
+      if (k >= width) break;  // never for the pattern the layout was built from
       const int64_t E = base + (int64_t)k * kSlice + lane;
       cols_out[E] = c;
       for (int q = 0; q < BB; ++q) {
@@ -359,6 +372,65 @@ int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const
   return GBPC_OK;
 }
 
+// Rows whose stored length exceeds the width of their slice.
+__global__ void sell_fits_kernel(int nrow, const int32_t* __restrict__ len,
+                                 const int32_t* __restrict__ perm,
+                                 const int64_t* __restrict__ slice_ptr, int32_t* bad) {
+  const int k_row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k_row >= nrow) return;
+  const int sl = k_row / kSlice;
+  const int r = perm ? perm[k_row] : k_row;
+  const int64_t width = (slice_ptr[sl + 1] - slice_ptr[sl]) / kSlice;
+  if (len[r] > width) atomicAdd(bad, 1);
+}
+
+// New values for an unchanged pattern: the fill pass again over the existing
+// layout (slices, row order, columns), writing vals in place, so captured
+// products see them.  Rejects a pattern whose rows do not fit the layout.
+int sell_refill(Sell& s, const int32_t* off, const int32_t* col, const void* val, int in_dtype,
+                const SellBuild& opt, cudaStream_t st) {
+  const int out_dtype = s.vdtype;
+  if (!valid_value_dtype(in_dtype) || (in_dtype == GBPC_BF16 && out_dtype != GBPC_BF16)) {
+    gbpc_set_error("unsupported value dtype %d -> %d", in_dtype, out_dtype);
+    return GBPC_ERR_ARG;
+  }
+  if (s.nrow > 0) {
+    DevBuf len, bad;
+    int rc;
+    if ((rc = len.alloc(sizeof(int32_t) * (s.nrow + 1)))) return rc;
+    if ((rc = bad.alloc(sizeof(int32_t)))) return rc;
+    GBPC_CUDA_TRY(cudaMemsetAsync(bad.p, 0, sizeof(int32_t), st));
+    sell_length_kernel<<<grid_for(s.nrow, kThreads), kThreads, 0, st>>>(
+        s.nrow, off, col, opt.rows, opt.colmap, opt.part, len.as<int32_t>());
+    sell_fits_kernel<<<grid_for(s.nrow, kThreads), kThreads, 0, st>>>(
+        s.nrow, len.as<int32_t>(), s.perm.p ? s.perm.as<int32_t>() : nullptr,
+        s.slice_ptr.as<int64_t>(), bad.as<int32_t>());
+    GBPC_CUDA_TRY(cudaGetLastError());
+    int32_t h = 0;
+    GBPC_CUDA_TRY(cudaMemcpyAsync(&h, bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h) {
+      gbpc_set_error("refill: %d rows do not fit the operator's layout (pattern changed)", h);
+      return GBPC_ERR_ARG;
+    }
+  }
+  if (s.nslices > 0) {
+    if (in_dtype == GBPC_BF16) {
+      launch_fill<__nv_bfloat16, __nv_bfloat16>(s, s.B, off, col, val, opt, st);
+    } else if (in_dtype == GBPC_F64) {
+      if (out_dtype == GBPC_F64) launch_fill<double, double>(s, s.B, off, col, val, opt, st);
+      else if (out_dtype == GBPC_F32) launch_fill<double, float>(s, s.B, off, col, val, opt, st);
+      else launch_fill<double, __nv_bfloat16>(s, s.B, off, col, val, opt, st);
+    } else {
+      if (out_dtype == GBPC_F64) launch_fill<float, double>(s, s.B, off, col, val, opt, st);
+      else if (out_dtype == GBPC_F32) launch_fill<float, float>(s, s.B, off, col, val, opt, st);
+      else launch_fill<float, __nv_bfloat16>(s, s.B, off, col, val, opt, st);
+    }
+  }
+  GBPC_CUDA_TRY(cudaGetLastError());
+  return GBPC_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Product entry point (kernels in gbpc_spmv.cuh, instantiated per vector type
 // in gbpc_spmv_f64.cu and gbpc_spmv_f32.cu).
@@ -398,7 +470,7 @@ int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, 
 
 // Kernel variants timed by the autotuner (scalar rows; must match
 // launch_variant in gbpc_spmv.cuh).
-constexpr int kNumVariants = 3;
+constexpr int kNumVariants = 4;
 
 int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
   if (m.B != 1 || m.nslices == 0) {

@@ -37,10 +37,65 @@ template <> struct Chunk<2> { static constexpr int value = 4; };
 template <> struct Chunk<3> { static constexpr int value = 2; };
 template <> struct Chunk<4> { static constexpr int value = 1; };
 
+// Epilogue of one row: z[row] from the accumulated product (and the fused
+// dot contribution, in row order of the calling thread).
+template <int B, typename V, typename A, int EPI, bool DOT>
+__device__ __forceinline__ void spmv_finish(const SellView<V>& m, int row, const A (&acc)[B],
+                                            const A* y, A* z, A alpha, A beta, bool run,
+                                            bool alpha_one, bool beta_zero, const EpiDev<A>& ep,
+                                            const Reduction& red, double& dot_part) {
+  constexpr int BB = B * B;
+  if (row < m.nrow) {
+    const int orow = m.perm ? __ldg(m.perm + row) : row;
+    A out[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const int64_t idx = (int64_t)orow * B + r;
+      if (EPI == EPI_AXPBY) {
+        A v = alpha_one ? acc[r] : alpha * acc[r];
+        if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
+        out[r] = v;
+      } else if (EPI == EPI_SQLAP_BWD) {
+        A v = A(0);
+        if (run) {
+          v = fma_t<A>(ep.aux0[idx], ep.aux1[idx], acc[r]);
+          if (!alpha_one) v = alpha * v;
+        }
+        if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
+        out[r] = v;
+      } else if (EPI == EPI_SQLAP_FWD) {
+        out[r] = ep.aux0[idx] * acc[r];
+      } else {
+        out[r] = ep.aux0[idx] - acc[r];
+      }
+    }
+    if (EPI == EPI_TRI_UPPER) {
+      A t[B];
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        A s2 = A(0);
+#pragma unroll
+        for (int q = 0; q < B; ++q) s2 = fma_t<A>(ep.aux1[(int64_t)orow * BB + r * B + q], out[q], s2);
+        t[r] = s2;
+      }
+#pragma unroll
+      for (int r = 0; r < B; ++r) out[r] = t[r];
+    }
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const int64_t idx = (int64_t)orow * B + r;
+      z[idx] = out[r];
+      if (DOT) dot_part = fma((double)out[r], red.w[idx], dot_part);
+    }
+  }
+}
+
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB)
 sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
                  const int* guard, EpiDev<A> ep, Reduction red) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (guard_off(guard)) return;
   constexpr int BB = B * B;
   const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
@@ -90,49 +145,77 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
         }
       }
     }
-    if (row < m.nrow) {
-      const int orow = m.perm ? __ldg(m.perm + row) : row;
-      A out[B];
+    spmv_finish<B, V, A, EPI, DOT>(m, row, acc, y, z, alpha, beta, run, alpha_one, beta_zero, ep,
+                                   red, dot_part);
+  }
+  if (DOT) reduce_and_finalize(red, dot_part);
+}
+
+// Scalar rows, two slices at once: the slices s and s + (warps in the grid)
+// that the loop above would take one after the other are read together, so
+// every lane keeps two independent FMA chains and twice the loads in flight.
+// Each row still sums its entries in storage order, and the dot product
+// receives the rows in the same order, so the result equals the one-slice
+// kernel's bit for bit.
+template <typename V, typename A, int EPI, bool DOT, int CH>
+__global__ void __launch_bounds__(kThreads, 1)
+sell_spmv2_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
+                  const int* guard, EpiDev<A> ep, Reduction red) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (guard_off(guard)) return;
+  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  double dot_part = 0.0;
+  for (int s = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; s < m.nslices; s += 2 * warps_total) {
+    const int s2 = s + warps_total;
+    const bool has2 = s2 < m.nslices;  // uniform across the warp
+    const int64_t base1 = __ldg(m.slice_ptr + s);
+    const int width1 = (int)((__ldg(m.slice_ptr + s + 1) - base1) >> 5);
+    int64_t base2 = 0;
+    int width2 = 0;
+    if (has2) {
+      base2 = __ldg(m.slice_ptr + s2);
+      width2 = (int)((__ldg(m.slice_ptr + s2 + 1) - base2) >> 5);
+    }
+    A acc1[1] = {A(0)}, acc2[1] = {A(0)};
+    if (run) {
+      const int32_t* cp1 = m.cols + base1 + lane;
+      const V* vp1 = m.vals + base1 + lane;
+      const int32_t* cp2 = m.cols + base2 + lane;
+      const V* vp2 = m.vals + base2 + lane;
+      const int wmax = max(width1, width2);
+      for (int k0 = 0; k0 < wmax; k0 += CH) {
+        int c1[CH], c2[CH];
 #pragma unroll
-      for (int r = 0; r < B; ++r) {
-        const int64_t idx = (int64_t)orow * B + r;
-        if (EPI == EPI_AXPBY) {
-          A v = alpha_one ? acc[r] : alpha * acc[r];
-          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
-          out[r] = v;
-        } else if (EPI == EPI_SQLAP_BWD) {
-          A v = A(0);
-          if (run) {
-            v = fma_t<A>(ep.aux0[idx], ep.aux1[idx], acc[r]);
-            if (!alpha_one) v = alpha * v;
-          }
-          if (!beta_zero) v = fma_t<A>(beta, y[idx], v);
-          out[r] = v;
-        } else if (EPI == EPI_SQLAP_FWD) {
-          out[r] = ep.aux0[idx] * acc[r];
-        } else {
-          out[r] = ep.aux0[idx] - acc[r];
+        for (int j = 0; j < CH; ++j) {
+          c1[j] = (k0 + j < width1) ? __ldg(cp1 + (int64_t)(k0 + j) * kSlice) : -1;
+          c2[j] = (k0 + j < width2) ? __ldg(cp2 + (int64_t)(k0 + j) * kSlice) : -1;
         }
-      }
-      if (EPI == EPI_TRI_UPPER) {
-        A t[B];
+        A x1[CH], x2[CH];
+        V v1[CH], v2[CH];
 #pragma unroll
-        for (int r = 0; r < B; ++r) {
-          A s2 = A(0);
-#pragma unroll
-          for (int q = 0; q < B; ++q) s2 = fma_t<A>(ep.aux1[(int64_t)orow * BB + r * B + q], out[q], s2);
-          t[r] = s2;
+        for (int j = 0; j < CH; ++j) {
+          x1[j] = (c1[j] >= 0) ? __ldg(x + c1[j]) : A(0);
+          x2[j] = (c2[j] >= 0) ? __ldg(x + c2[j]) : A(0);
+          v1[j] = (k0 + j < width1) ? __ldg(vp1 + (int64_t)(k0 + j) * kSlice) : static_cast<V>(0.0f);
+          v2[j] = (k0 + j < width2) ? __ldg(vp2 + (int64_t)(k0 + j) * kSlice) : static_cast<V>(0.0f);
         }
 #pragma unroll
-        for (int r = 0; r < B; ++r) out[r] = t[r];
-      }
-#pragma unroll
-      for (int r = 0; r < B; ++r) {
-        const int64_t idx = (int64_t)orow * B + r;
-        z[idx] = out[r];
-        if (DOT) dot_part = fma((double)out[r], red.w[idx], dot_part);
+        for (int j = 0; j < CH; ++j) {
+          if (k0 + j < width1) acc1[0] = fma_t<A>(widen<A, V>(v1[j]), x1[j], acc1[0]);
+          if (k0 + j < width2) acc2[0] = fma_t<A>(widen<A, V>(v2[j]), x2[j], acc2[0]);
+        }
       }
     }
+    spmv_finish<1, V, A, EPI, DOT>(m, s * kSlice + lane, acc1, y, z, alpha, beta, run, alpha_one,
+                                   beta_zero, ep, red, dot_part);
+    if (has2)
+      spmv_finish<1, V, A, EPI, DOT>(m, s2 * kSlice + lane, acc2, y, z, alpha, beta, run,
+                                     alpha_one, beta_zero, ep, red, dot_part);
   }
   if (DOT) reduce_and_finalize(red, dot_part);
 }
@@ -159,17 +242,17 @@ static int spmv_flags(double alpha, double beta) {
   return f;
 }
 
-// Product kernel variants for scalar rows differ in the entries loaded per
-// chunk (8, 16, 4); all have a 64-register budget (one 1024-thread CTA per
-// SM).  Blocked rows use one variant.
-constexpr int kNumVariants = 3;
+// Product kernel variants for scalar rows: entries loaded per chunk 8, 16,
+// 4, and 3 on each of two slices at once; all have a 64-register budget
+// (one 1024-thread CTA per SM).  Blocked rows use one variant.
+constexpr int kNumVariants = 4;
 
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
 static void launch_one(const SellView<V>& view, const void* x, const void* y, void* z,
                        double alpha, double beta, int flags, const int* guard, const EpiDev<A>& e,
                        const Reduction& red, int nslices, cudaStream_t st) {
-  sell_spmv_kernel<B, V, A, EPI, DOT, CH, MINB><<<spmv_grid(nslices, MINB), kThreads, 0, st>>>(
-      view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+  launch_k(sell_spmv_kernel<B, V, A, EPI, DOT, CH, MINB>, spmv_grid(nslices, MINB), kThreads, 0,
+           st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
 }
 
 template <int B, typename V, typename A, int EPI, bool DOT>
@@ -186,6 +269,10 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
       case 2:
         launch_one<B, V, A, EPI, DOT, 4, 1>(view, x, y, z, alpha, beta, flags, guard, e, red,
                                             nslices, st);
+        return;
+      case 3:
+        launch_k(sell_spmv2_kernel<V, A, EPI, DOT, 3>, spmv_grid(nslices, 1), kThreads, 0, st,
+                 view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
         return;
       default:
         break;

@@ -73,7 +73,9 @@ class FSAI(LinearOperator):
     matrix (products still accumulate in float64), or bfloat16 (an addition of
     this build for the mixed-precision path).  ``apply_lanes`` is validated for
     compatibility; the apply kernel's layout is chosen by the library.
-    Setup synchronises; apply is stream-ordered and graph-capturable.
+    Setup synchronises; apply is stream-ordered and graph-capturable.  With
+    ``reuse_pattern=True``, ``update(A)`` refits the original supports for new
+    values on the same topology (fsai_reuse.py).
     """
 
     def __init__(self, A, max_row_size=8, kap_tolerance=1.0e-3, pivot_floor=None, apply_lanes=1,
@@ -105,8 +107,6 @@ class FSAI(LinearOperator):
             raise ValueError(
                 "factor_dtype must be the matrix scalar type, or torch.float32 for a float64 matrix"
             )
-        if reuse_pattern:
-            raise NotImplementedError("reuse_pattern (fixed-support refit) is not available yet")
         self.max_row_size = max_row_size
         self.max_step_size = max_step_size
         self.factor_dtype = factor_dtype
@@ -134,7 +134,114 @@ class FSAI(LinearOperator):
             _lib.ptr(self.GT.values), _lib.dtype_code(factor_dtype), _lib.dtype_code(dt),
             _lib.stream(A.device))
         super().__init__(A.shape, dt, A.device, self._apply)
+        self._refit = _RefitPlan(self, A, max_row_size, pivot_floor) if reuse_pattern else None
+
+    def update(self, A=None):
+        """Refit on the original factor supports (fsai.py:346-362).
+
+        Requires ``reuse_pattern=True`` and the topology the factor was built
+        from.  This is not a new adaptive pattern search; rebuild when
+        convergence worsens.  A failed validation leaves the previous factor
+        intact.  G and GT keep their storage, so captured applies see the new
+        values.  Synchronises.
+        """
+        if self._refit is None:
+            raise ValueError("Construct FSAI with reuse_pattern=True before updating")
+        A = self.source if A is None else A
+        if not isinstance(A, BsrMatrix):
+            raise ValueError("update requires a BsrMatrix")
+        self._refit.update(self, A)
+        self.source = A
+        return self
+
+    def quality(self, A=None, probes=4, seed=17):
+        """Rademacher estimate of ``||G A G^T - I||_F / sqrt(n)`` with fixed
+        random probes (fsai_reuse.py:248-279): a diagnostic, not a bound on
+        conditioning or iterations.  The probes come from torch's generator,
+        so a seed does not give the reference's probe vectors.  Allocates
+        and synchronises; not capturable."""
+        if isinstance(probes, bool) or not isinstance(probes, int) or probes < 1:
+            raise ValueError("probes must be a positive integer")
+        A = self.source if A is None else A
+        if (not isinstance(A, BsrMatrix)
+                or (A.shape, A.dtype, A.device) != (self.shape, self.dtype, self.device)):
+            raise ValueError("quality requires matching shape, dtype and device")
+        n = A.shape[0]
+        if n == 0:
+            return 0.0
+        from .linear import aslinearoperator
+
+        dt = A.scalar_type
+        g_op, gt_op = _product_op(self.G, dt), _product_op(self.GT, dt)
+        a_op = aslinearoperator(A)
+        x, y, z, w = (torch.empty(n, dtype=dt, device=A.device) for _ in range(4))
+        gen = torch.Generator()
+        total = 0.0
+        for p in range(probes):
+            gen.manual_seed(seed + p)
+            x.copy_(torch.randint(0, 2, (n,), generator=gen).to(dt) * 2 - 1)
+            gt_op.apply(x, None, y, 1.0, 0.0, A.device)
+            a_op.matvec(y, None, z, 1.0, 0.0)
+            g_op.apply(z, None, w, 1.0, 0.0, A.device)
+            w -= x
+            total += float(torch.dot(w, w))
+        return (total / (probes * max(n, 1))) ** 0.5
 
     def _apply(self, x, y, z, alpha, beta):
         self._op.apply(x.reshape(-1), y.reshape(-1) if y is not None else None, z.view(-1),
                        alpha, beta, self.device)
+
+
+def _product_op(M: BsrMatrix, vector_dtype) -> _lib.OpHandle:
+    """Plain product with M (scalar CSR) on vectors of `vector_dtype`."""
+    return _lib.new_op("gbpc_op_sparse", M.nrow, M.ncol, 1, _lib.ptr(M.offsets),
+                       _lib.ptr(M.columns), _lib.ptr(M.values), _lib.dtype_code(M.scalar_type),
+                       _lib.dtype_code(vector_dtype), _lib.stream(M.device))
+
+
+class _RefitPlan:
+    """Fixed-support refit state (fsai_reuse.py:157-245, ``RefitPlan``): the
+    source topology to compare against, the position of every G entry in
+    G^T, and a candidate buffer that replaces G's values only when every row
+    of the refit is valid."""
+
+    def __init__(self, owner: FSAI, A: BsrMatrix, width: int, floor: float):
+        self.signature = (A.shape, A.block_shape, A.scalar_type, A.device)
+        self.offsets = A.offsets.clone()
+        self.columns = A.columns.clone()
+        self.width, self.floor = width, float(floor)
+        G, GT = owner.G, owner.GT
+        self.transpose = torch.empty(max(G.nnz, 1), dtype=torch.int32, device=A.device)
+        if G.nnz:
+            _lib.call("gbpc_transpose_map", G.nrow, _lib.ptr(G.offsets), _lib.ptr(G.columns),
+                      _lib.ptr(GT.offsets), _lib.ptr(GT.columns), _lib.ptr(self.transpose),
+                      _lib.stream(A.device))
+        self.candidate = torch.empty_like(G.values)
+
+    def update(self, owner: FSAI, A: BsrMatrix) -> None:
+        if (A.shape, A.block_shape, A.scalar_type, A.device) != self.signature:
+            raise ValueError("FSAI update requires the original shape, dtype, device and topology")
+        if A.offsets.shape != self.offsets.shape or A.columns.shape != self.columns.shape:
+            raise ValueError("FSAI update requires identical topology storage")
+        if not (torch.equal(A.offsets, self.offsets) and torch.equal(A.columns, self.columns)):
+            raise ValueError("FSAI update requires identical sparsity; rebuild to change it")
+        if A.values.numel() < self.columns.numel() * A.block_size:
+            raise ValueError("Insufficient source values")
+        G, GT = owner.G, owner.GT
+        if G.nrow == 0:
+            return
+        scalar = scalarize(A)
+        st = _lib.stream(A.device)
+        status = (ctypes.c_int32 * 2)()
+        _lib.call("gbpc_fsai_refit", G.nrow, _lib.ptr(scalar.offsets), _lib.ptr(scalar.columns),
+                  _lib.ptr(scalar.values.reshape(-1)), _lib.dtype_code(scalar.scalar_type),
+                  _lib.ptr(G.offsets), _lib.ptr(G.columns), self.width, self.floor,
+                  _lib.ptr(self.candidate), _lib.dtype_code(G.scalar_type), status, st)
+        if status[0] or status[1]:
+            raise ValueError("FSAI refit requires finite positive diagonals and SPD local supports")
+        G.values.copy_(self.candidate)
+        _lib.call("gbpc_scatter_values", G.nnz, _lib.ptr(G.values), _lib.ptr(self.transpose),
+                  _lib.ptr(GT.values), _lib.dtype_code(G.scalar_type), st)
+        _lib.call("gbpc_op_fsai_refill", owner._op.handle, _lib.ptr(G.offsets),
+                  _lib.ptr(G.columns), _lib.ptr(G.values), _lib.ptr(GT.offsets),
+                  _lib.ptr(GT.columns), _lib.ptr(GT.values), _lib.dtype_code(G.scalar_type), st)
