@@ -323,6 +323,23 @@ int gbpc_solver_destroy(gbpc_solver* solver);
 /* Device bytes of the solver's Krylov state (work vectors, scalars). */
 int gbpc_solver_device_bytes(const gbpc_solver* solver, size_t* bytes_host);
 
+/* Restarted right-preconditioned GMRES(restart), restart <= 64: replaces
+ * warp.optim.linear.gmres at the reference's call sites
+ * (tests/test_biharmonic.py:32, tests/test_indefinite.py:130,
+ * benchmarks/indefinite.py:192-225).  Arnoldi on A M with classical
+ * Gram-Schmidt applied twice, Givens rotations, stop when the residual norm
+ * |b - A x| (the Givens estimate) <= max(atol, tol |b|) or after maxiter
+ * Arnoldi steps (maxiter <= 0: the vector length).  One CUDA graph per
+ * (b, x) pair when use_graph != 0.  nit_dev / res_dev / target_dev
+ * (optional) receive the steps, the final residual norm and the target. */
+typedef struct gbpc_gmres gbpc_gmres;
+int gbpc_gmres_create(gbpc_op* A, gbpc_op* M, int restart, void* stream, gbpc_gmres** out);
+int gbpc_gmres_run(gbpc_gmres* solver, const double* b, double* x, double tol, double atol,
+                   int maxiter, int use_graph, int32_t* nit_dev, double* res_dev,
+                   double* target_dev, void* stream);
+int gbpc_gmres_device_bytes(const gbpc_gmres* solver, size_t* bytes_host);
+int gbpc_gmres_destroy(gbpc_gmres* solver);
+
 /* ------------------------------------------------------------------------ */
 /* Many right-hand sides: batched operators, batched PCG, mixed-precision     */
 /* iterative refinement (no reference counterpart: the reference solves one   */

@@ -411,5 +411,84 @@ def krylov(method, A: Operator, b, x0=None, M: Operator | None = None, tol=1e-8,
     return x, int(it), rr.value, atol_sq.value
 
 
+def gmres(A: Operator, b, x0=None, M: Operator | None = None, tol=1e-5, atol=0.0, restart=31,
+          maxiter=0):
+    """Textbook restarted right-preconditioned GMRES(restart) in numpy (small
+    cases): Arnoldi on A M with classical Gram-Schmidt applied twice, Givens
+    rotations, stop when |g_{j+1}| <= max(atol, tol |b|) or after `maxiter`
+    Arnoldi steps, then x += M (V y).  The call semantics of
+    warp.optim.linear.gmres at the reference's call sites
+    (tests/test_biharmonic.py:32, tests/test_indefinite.py:130).  Returns
+    (x, steps, residual norm, target)."""
+    b = np.ascontiguousarray(b, np.float64).reshape(-1)
+    n = b.size
+    x = np.zeros(n) if x0 is None else np.ascontiguousarray(x0, np.float64).reshape(-1).copy()
+    maxiter = maxiter if maxiter > 0 else max(n, 1)
+    target = max(atol, tol * np.sqrt(b @ b))
+    zero = np.zeros(n)
+    op_a = lambda v: A.apply(v, zero, 1.0, 0.0)
+    op_m = (lambda v: M.apply(v, zero, 1.0, 0.0)) if M is not None else (lambda v: v.copy())
+    m, it = restart, 0
+    r = b - op_a(x)
+    beta = np.sqrt(r @ r)
+    res = beta
+    while beta * beta > target * target and np.isfinite(beta) and beta > 0 and it < maxiter:
+        V = np.zeros((m + 1, n))
+        V[0] = r / beta
+        H = np.zeros((m + 1, m))
+        cs, sn = np.zeros(m), np.zeros(m)
+        g = np.zeros(m + 1)
+        g[0] = beta
+        k, stop = 0, False
+        for j in range(m):
+            w = op_a(op_m(V[j]))
+            h = V[:j + 1] @ w
+            w = w - h @ V[:j + 1]
+            h2 = V[:j + 1] @ w
+            w = w - h2 @ V[:j + 1]
+            h = h + h2
+            hn = np.sqrt(w @ w)
+            H[:j + 1, j] = h
+            H[j + 1, j] = hn
+            for i in range(j):
+                a_, b_ = H[i, j], H[i + 1, j]
+                H[i, j] = cs[i] * a_ + sn[i] * b_
+                H[i + 1, j] = -sn[i] * a_ + cs[i] * b_
+            a_, b_ = H[j, j], H[j + 1, j]
+            c, s_ = 1.0, 0.0
+            if b_ != 0.0:
+                if abs(b_) > abs(a_):
+                    t = a_ / b_
+                    s_ = 1.0 / np.sqrt(1.0 + t * t)
+                    c = s_ * t
+                else:
+                    t = b_ / a_
+                    c = 1.0 / np.sqrt(1.0 + t * t)
+                    s_ = c * t
+            cs[j], sn[j] = c, s_
+            H[j, j] = c * a_ + s_ * b_
+            H[j + 1, j] = 0.0
+            g[j + 1] = -s_ * g[j]
+            g[j] = c * g[j]
+            res = abs(g[j + 1])
+            it += 1
+            k = j + 1
+            stop = res * res <= target * target or it >= maxiter
+            if stop or not (hn > 0 and np.isfinite(hn)) or j + 1 == m:
+                break
+            V[j + 1] = w / hn
+        y = np.zeros(k)
+        for i in range(k - 1, -1, -1):
+            t = g[i] - H[i, i + 1:k] @ y[i + 1:k]
+            y[i] = t / H[i, i] if H[i, i] != 0.0 else 0.0
+        x = x + op_m(V[:k].T @ y)
+        if stop:
+            break
+        r = b - op_a(x)
+        beta = np.sqrt(r @ r)
+        res = beta
+    return x, it, float(res), float(target)
+
+
 if os.environ.get("GBPC_ORACLE_THREADS"):
     set_threads(int(os.environ["GBPC_ORACLE_THREADS"]))

@@ -7,7 +7,7 @@ libgbpc.so reached through its C ABI (include/gbpc.h):
     FSAI, SparseOperator, SquaredLaplacianOperator, BlockJacobi, BlockILU0,
     BiharmonicSystem, RepeatedFSAI, BlockFSAI, BsrBlockFSAI
 
-plus ``linear.cg`` / ``linear.cr`` / ``linear.preconditioner`` and the
+plus ``linear.cg`` / ``linear.cr`` / ``linear.gmres`` / ``linear.preconditioner`` and the
 ``sparse`` helpers that stand in for warp.optim.linear and warp.sparse.
 Vectors and matrices are torch CUDA tensors.
 """
@@ -17,7 +17,7 @@ from .biharmonic import BiharmonicSystem, RepeatedFSAI
 from .block_fsai import BlockFSAI, BsrBlockFSAI
 from .block_ilu import BlockILU0, BlockJacobi
 from .fsai import FSAI
-from .linear import LinearOperator, aslinearoperator, cg, cr, preconditioner
+from .linear import LinearOperator, aslinearoperator, cg, cr, gmres, preconditioner
 from .sparse import BsrMatrix, bsr_copy, bsr_from_triplets, bsr_transposed, from_scipy
 from .sparse_operator import SparseOperator
 from .squared_laplacian import SquaredLaplacianOperator
@@ -40,6 +40,7 @@ __all__ = [
     "bsr_transposed",
     "cg",
     "cr",
+    "gmres",
     "from_scipy",
     "batched",
     "linear",

@@ -5,8 +5,7 @@
 ``H = M + sqrt(tau) K``; ``preconditioner(**fsai_options)`` returns
 ``RepeatedFSAI(FSAI(H))``, which applies the scalar FSAI to both components
 of vec2 arrays through 2 x 2 block products of ``diag(G, G)``.  The lifted
-system is nonsymmetric (GMRES territory); this build keeps the constructors
-and operators so the API is intact.
+system is nonsymmetric: solve it with ``linear.gmres`` (never CG/CR).
 """
 
 from __future__ import annotations

@@ -1,0 +1,673 @@
+// Restarted, right-preconditioned GMRES(m) with the whole loop on the device.
+//
+// warp.optim.linear.gmres (warp-lang, not vendored) is what the reference's
+// lifted-biharmonic and indefinite call sites use (tests/test_biharmonic.py:32,
+// tests/test_indefinite.py:130, benchmarks/indefinite.py:192-225).  Its exact
+// iterates are not pinned by the reference; this is the textbook method:
+// Arnoldi on A M with classical Gram-Schmidt applied twice (each pass one
+// multi-dot and one multi-axpy over the basis), Givens rotations on the
+// Hessenberg column, the residual norm |g_{j+1}| as the stopping quantity
+// (stop when it is <= max(atol, tol |b|) or after maxiter steps), and at the
+// end of a cycle x += M (V y) with H y = g solved by back-substitution.
+//
+// One CUDA graph: initialisation (r = b - A x, v_0 = r/|r|), then a
+// conditional while-node whose body is one Arnoldi step followed by a
+// conditional if-node holding the end-of-cycle update (back-substitution,
+// solution update, new residual).  Every reduction is deterministic: per-CTA
+// partials combined in index order by the last CTA to finish.
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "gbpc_common.cuh"
+#include "gbpc_internal.h"
+
+namespace gbpc {
+
+int copy_with_dot(int64_t n, const double* x, double* z, const int* guard, const Reduction& red,
+                  cudaStream_t st);
+
+namespace {
+
+constexpr int kGT = 256;          // threads per CTA
+constexpr int kGMaxK = 65;        // basis vectors (restart <= 64)
+constexpr int kGCtas = 152 * 4;   // CTAs of the vector kernels (at most)
+
+struct GmresState {
+  int m, j, it, maxiter;
+  int done, not_done, restart, resid;  // flags (ints: operator guards point at them)
+  double tol, atol, atol_sq, bb, beta2, ww, res, inv;
+  unsigned long long while_handle, if_handle;
+};
+
+// Hessenberg workspace: H column-major (m+1) x m, rotations, g, y, the
+// current column and the coefficients of the last Gram-Schmidt pass.
+struct GmresWork {
+  double* H;
+  double* cs;
+  double* sn;
+  double* g;
+  double* y;
+  double* hcol;
+  double* coef;
+};
+
+__device__ __forceinline__ void set_cond(unsigned long long h, bool v) {
+  if (h != 0ull) cudaGraphSetConditional((cudaGraphConditionalHandle)h, v ? 1u : 0u);
+}
+
+int g_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kGT - 1) / kGT, kGCtas)); }
+
+// Sum of a value over the CTA (kGT threads), valid in thread 0.
+__device__ __forceinline__ double cta_sum(double v, double* sm) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kGT / 32; ++w) s += sm[w];
+  __syncthreads();
+  return s;
+}
+
+// Last CTA to arrive gets true (after its partial is visible).
+__device__ __forceinline__ bool arrive_last(unsigned int* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+__global__ void gm_setup_kernel(GmresState* s, int m, double tol, double atol, int maxiter,
+                                unsigned long long while_handle, unsigned long long if_handle) {
+  s->m = m;
+  s->j = 0;
+  s->it = 0;
+  s->maxiter = maxiter;
+  s->done = 0;
+  s->not_done = 1;
+  s->restart = 0;
+  s->resid = 1;
+  s->tol = tol;
+  s->atol = atol;
+  s->res = 0.0;
+  s->while_handle = while_handle;
+  s->if_handle = if_handle;
+}
+
+// bb = b.b, then atol_sq = max(atol, tol |b|)^2.
+__global__ void __launch_bounds__(kGT)
+gm_bnorm_kernel(int64_t n, const double* b, GmresState* s, double* partials,
+                unsigned int* counter) {
+  __shared__ double sm[kGT / 32];
+  double acc = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT)
+    acc = fma(b[r], b[r], acc);
+  const double cs = cta_sum(acc, sm);
+  if (threadIdx.x == 0) partials[blockIdx.x] = cs;
+  if (arrive_last(counter) && threadIdx.x == 0) {
+    double t = 0.0;
+    for (unsigned c = 0; c < gridDim.x; ++c) t += __ldcg(partials + c);
+    s->bb = t;
+    const double a = fmax(s->atol, s->tol * sqrt(t));
+    s->atol_sq = a * a;
+    *counter = 0u;
+  }
+}
+
+// coef[i] = V_i . w for i <= j (this pass); hcol accumulates the passes.
+__global__ void __launch_bounds__(kGT)
+gm_mdot_kernel(int64_t n, const double* V, const double* w, GmresState* s, GmresWork wk,
+               int accumulate, double* partials, unsigned int* counter) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (*(volatile int*)&s->not_done == 0) return;
+  __shared__ double sm[kGT / 32][kGMaxK];
+  const int k = s->j + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = 0; i < k; ++i) {
+    const double* Vi = V + (size_t)i * n;
+    double acc = 0.0;
+    for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT)
+      acc = fma(Vi[r], w[r], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) sm[warp][i] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double t = 0.0;
+    for (int q = 0; q < kGT / 32; ++q) t += sm[q][threadIdx.x];
+    partials[(size_t)blockIdx.x * kGMaxK + threadIdx.x] = t;
+  }
+  if (arrive_last(counter)) {
+    if (threadIdx.x < k) {
+      double t = 0.0;
+      for (unsigned c = 0; c < gridDim.x; ++c) t += __ldcg(partials + (size_t)c * kGMaxK + threadIdx.x);
+      wk.coef[threadIdx.x] = t;
+      wk.hcol[threadIdx.x] = accumulate ? wk.hcol[threadIdx.x] + t : t;
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+  }
+}
+
+// Givens update of column j and the stopping test (one thread).
+__device__ void gm_step_finalize(GmresState* s, GmresWork wk, double ww) {
+  const int j = s->j, m = s->m;
+  double* H = wk.H + (size_t)j * (m + 1);
+  for (int i = 0; i <= j; ++i) H[i] = wk.hcol[i];
+  const double hn = sqrt(ww);
+  H[j + 1] = hn;
+  for (int i = 0; i < j; ++i) {
+    const double a = H[i], b = H[i + 1];
+    H[i] = wk.cs[i] * a + wk.sn[i] * b;
+    H[i + 1] = -wk.sn[i] * a + wk.cs[i] * b;
+  }
+  const double a = H[j], b = H[j + 1];
+  double c = 1.0, sn = 0.0;
+  if (b != 0.0) {
+    if (fabs(b) > fabs(a)) {
+      const double t = a / b;
+      sn = 1.0 / sqrt(1.0 + t * t);
+      c = sn * t;
+    } else {
+      const double t = b / a;
+      c = 1.0 / sqrt(1.0 + t * t);
+      sn = c * t;
+    }
+  }
+  wk.cs[j] = c;
+  wk.sn[j] = sn;
+  H[j] = c * a + sn * b;
+  H[j + 1] = 0.0;
+  const double gj = wk.g[j];
+  wk.g[j + 1] = -sn * gj;
+  wk.g[j] = c * gj;
+  s->res = fabs(wk.g[j + 1]);
+  s->it += 1;
+  const bool breakdown = !(hn > 0.0) || !isfinite(hn);
+  s->inv = breakdown ? 0.0 : 1.0 / hn;
+  const bool conv = s->res * s->res <= s->atol_sq;
+  const bool stop = conv || s->it >= s->maxiter;
+  const bool restart = stop || breakdown || (j + 1 == m);
+  s->done = stop;
+  s->not_done = !stop;
+  s->restart = restart;
+  s->resid = restart && !stop;
+  set_cond(s->if_handle, restart);
+  set_cond(s->while_handle, !stop);
+}
+
+// w -= sum_i coef[i] V_i; with `norm`, ww = w.w and the step finalize.
+__global__ void __launch_bounds__(kGT)
+gm_update_kernel(int64_t n, const double* V, double* w, GmresState* s, GmresWork wk, int norm,
+                 double* partials, unsigned int* counter) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (*(volatile int*)&s->not_done == 0) return;
+  __shared__ double sm[kGT / 32];
+  __shared__ double cf[kGMaxK];
+  const int k = s->j + 1;
+  if (threadIdx.x < k) cf[threadIdx.x] = wk.coef[threadIdx.x];
+  __syncthreads();
+  double acc = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT) {
+    double v = w[r];
+    for (int i = 0; i < k; ++i) v = fma(-cf[i], V[(size_t)i * n + r], v);
+    w[r] = v;
+    acc = fma(v, v, acc);
+  }
+  if (!norm) return;
+  const double c = cta_sum(acc, sm);
+  if (threadIdx.x == 0) partials[blockIdx.x] = c;
+  if (arrive_last(counter) && threadIdx.x == 0) {
+    double t = 0.0;
+    for (unsigned q = 0; q < gridDim.x; ++q) t += __ldcg(partials + q);
+    s->ww = t;
+    gm_step_finalize(s, wk, t);
+    *counter = 0u;
+  }
+}
+
+// v_{j+1} = w / h_{j+1} into the basis and the fixed current vector, then j++
+// (the last CTA, after every CTA has read j).
+__global__ void __launch_bounds__(kGT)
+gm_next_kernel(int64_t n, double* V, const double* w, double* vcur, GmresState* s,
+               unsigned int* counter) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (*(volatile int*)&s->restart != 0 || *(volatile int*)&s->not_done == 0) return;
+  const int j1 = s->j + 1;
+  const double inv = s->inv;
+  double* Vn = V + (size_t)j1 * n;
+  for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT) {
+    const double v = w[r] * inv;
+    Vn[r] = v;
+    vcur[r] = v;
+  }
+  if (arrive_last(counter) && threadIdx.x == 0) {
+    s->j = j1;
+    *counter = 0u;
+  }
+}
+
+// End of a cycle: H y = g by back-substitution (one thread).
+__global__ void gm_solve_kernel(GmresState* s, GmresWork wk) {
+  if (*(volatile int*)&s->restart == 0) return;
+  const int k = s->j + 1, m = s->m;
+  for (int i = k - 1; i >= 0; --i) {
+    double t = wk.g[i];
+    for (int l = i + 1; l < k; ++l) t -= wk.H[(size_t)l * (m + 1) + i] * wk.y[l];
+    const double d = wk.H[(size_t)i * (m + 1) + i];
+    wk.y[i] = (d != 0.0) ? t / d : 0.0;
+  }
+}
+
+// t = sum_i y_i V_i
+__global__ void __launch_bounds__(kGT)
+gm_combine_kernel(int64_t n, const double* V, double* t, const GmresState* s, GmresWork wk) {
+  if (*(volatile const int*)&s->restart == 0) return;
+  __shared__ double yy[kGMaxK];
+  const int k = s->j + 1;
+  if (threadIdx.x < k) yy[threadIdx.x] = wk.y[threadIdx.x];
+  __syncthreads();
+  for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT) {
+    double v = 0.0;
+    for (int i = 0; i < k; ++i) v = fma(yy[i], V[(size_t)i * n + r], v);
+    t[r] = v;
+  }
+}
+
+// x += d
+__global__ void __launch_bounds__(kGT)
+gm_xupdate_kernel(int64_t n, double* x, const double* d, const GmresState* s) {
+  if (*(volatile const int*)&s->restart == 0) return;
+  for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT)
+    x[r] += d[r];
+}
+
+// After r = b - A x with beta2 = r.r: start a cycle (or stop).
+__global__ void gm_begin_kernel(GmresState* s, GmresWork wk) {
+  if (*(volatile int*)&s->resid == 0) return;
+  const double beta = sqrt(s->beta2);
+  for (int i = 0; i <= s->m; ++i) wk.g[i] = 0.0;
+  wk.g[0] = beta;
+  s->res = beta;
+  s->j = 0;
+  const bool conv = s->beta2 <= s->atol_sq;
+  const bool stop = conv || !(beta > 0.0) || !isfinite(beta) || s->it >= s->maxiter;
+  s->inv = stop ? 0.0 : 1.0 / beta;
+  s->done = stop;
+  s->not_done = !stop;
+  s->restart = 0;
+  set_cond(s->while_handle, !stop);
+}
+
+// v_0 = r / |r|
+__global__ void __launch_bounds__(kGT)
+gm_first_kernel(int64_t n, double* V, const double* r, double* vcur, const GmresState* s) {
+  if (*(volatile const int*)&s->not_done == 0) return;
+  const double inv = s->inv;
+  for (int64_t i = (int64_t)blockIdx.x * kGT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kGT) {
+    const double v = r[i] * inv;
+    V[i] = v;
+    vcur[i] = v;
+  }
+}
+
+__global__ void gm_outputs_kernel(const GmresState* s, int32_t* nit, double* res, double* target) {
+  if (nit) *nit = s->it;
+  if (res) *res = s->res;
+  if (target) *target = sqrt(s->atol_sq);
+}
+
+}  // namespace
+
+struct Gmres {
+  size_t device_bytes = 0;  // DevBuf bytes held (declared first: released last)
+  Operator* A = nullptr;
+  Operator* M = nullptr;
+  int64_t n = 0;
+  int m = 31;
+  DevBuf V, w, t, d, vcur, state, work, partials, counter;
+  ReduceBuf rb;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphConditionalHandle while_h = 0, if_h = 0;
+  const double* last_b = nullptr;
+  double* last_x = nullptr;
+
+  ~Gmres() { drop(); }
+  void drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    last_b = nullptr;
+    last_x = nullptr;
+  }
+  GmresState* S() { return state.as<GmresState>(); }
+  GmresWork W() {
+    double* base = work.as<double>();
+    GmresWork wk;
+    wk.H = base;
+    wk.cs = wk.H + (size_t)(m + 1) * m;
+    wk.sn = wk.cs + m;
+    wk.g = wk.sn + m;
+    wk.y = wk.g + (m + 1);
+    wk.hcol = wk.y + m;
+    wk.coef = wk.hcol + (m + 1);
+    return wk;
+  }
+  static size_t work_doubles(int m) { return (size_t)(m + 1) * m + 2 * (size_t)m + 2 * (size_t)(m + 1) + m + (m + 1); }
+
+  int precondition(const double* in, double* out, const int* guard, cudaStream_t st) {
+    if (M) return M->apply(in, nullptr, out, 1.0, 0.0, guard, nullptr, st);
+    GBPC_CUDA_TRY(cudaMemcpyAsync(out, in, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    return GBPC_OK;
+  }
+
+  // r = b - A x into w with beta2, then start a cycle.
+  int record_residual(const double* b, double* x, const int* guard, cudaStream_t st) {
+    DotSpec dot;
+    dot.w = w.as<double>();
+    dot.rb = &rb;
+    dot.mode = FIN_STORE;
+    dot.out = &S()->beta2;
+    int rc;
+    if ((rc = A->apply(x, b, w.p, -1.0, 1.0, guard, &dot, st))) return rc;
+    gm_begin_kernel<<<1, 1, 0, st>>>(S(), W());
+    gm_first_kernel<<<g_grid(n), kGT, 0, st>>>(n, V.as<double>(), w.as<double>(),
+                                                vcur.as<double>(), S());
+    GBPC_CUDA_TRY(cudaGetLastError());
+    return GBPC_OK;
+  }
+
+  int record_init(const double* b, double* x, cudaStream_t st) {
+    GBPC_CUDA_TRY(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), st));
+    gm_bnorm_kernel<<<g_grid(n), kGT, 0, st>>>(n, b, S(), partials.as<double>(),
+                                                counter.as<unsigned int>());
+    GBPC_CUDA_TRY(cudaGetLastError());
+    return record_residual(b, x, nullptr, st);
+  }
+
+  // One Arnoldi step: w = A M v_j, two Gram-Schmidt passes, Givens, v_{j+1}.
+  int record_step(cudaStream_t st) {
+    const int* guard = &S()->not_done;
+    int rc;
+    const double* in = vcur.as<double>();
+    if (M) {
+      if ((rc = M->apply(vcur.p, nullptr, t.p, 1.0, 0.0, guard, nullptr, st))) return rc;
+      in = t.as<double>();
+    }
+    if ((rc = A->apply(in, nullptr, w.p, 1.0, 0.0, guard, nullptr, st))) return rc;
+    for (int pass = 0; pass < 2; ++pass) {
+      GBPC_CUDA_TRY(launch_k(gm_mdot_kernel, g_grid(n), kGT, 0, st, n,
+                             (const double*)V.as<double>(), (const double*)w.as<double>(), S(), W(),
+                             pass, partials.as<double>(), counter.as<unsigned int>()));
+      GBPC_CUDA_TRY(launch_k(gm_update_kernel, g_grid(n), kGT, 0, st, n,
+                             (const double*)V.as<double>(), w.as<double>(), S(), W(), pass,
+                             partials.as<double>(), counter.as<unsigned int>()));
+    }
+    GBPC_CUDA_TRY(launch_k(gm_next_kernel, g_grid(n), kGT, 0, st, n, V.as<double>(),
+                           (const double*)w.as<double>(), vcur.as<double>(), S(),
+                           counter.as<unsigned int>()));
+    return GBPC_OK;
+  }
+
+  // End of a cycle: y, x += M (V y), and (unless finished) the next residual.
+  int record_cycle_end(const double* b, double* x, cudaStream_t st) {
+    int rc;
+    gm_solve_kernel<<<1, 1, 0, st>>>(S(), W());
+    gm_combine_kernel<<<g_grid(n), kGT, 0, st>>>(n, V.as<double>(), t.as<double>(), S(), W());
+    GBPC_CUDA_TRY(cudaGetLastError());
+    const double* dx = t.as<double>();
+    if (M) {
+      if ((rc = M->apply(t.p, nullptr, d.p, 1.0, 0.0, &S()->restart, nullptr, st))) return rc;
+      dx = d.as<double>();
+    }
+    gm_xupdate_kernel<<<g_grid(n), kGT, 0, st>>>(n, x, dx, S());
+    GBPC_CUDA_TRY(cudaGetLastError());
+    return record_residual(b, x, &S()->resid, st);
+  }
+
+  static int tail_of(cudaGraph_t g, cudaGraphNode_t* tail) {
+    size_t count = 0;
+    cudaGraphGetNodes(g, nullptr, &count);
+    std::vector<cudaGraphNode_t> nodes(count);
+    cudaGraphGetNodes(g, nodes.data(), &count);
+    *tail = nullptr;
+    for (auto nd : nodes) {
+      size_t outs = 0;
+      cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &outs);
+      if (outs == 0) *tail = nd;
+    }
+    return GBPC_OK;
+  }
+
+  int build_graph(const double* b, double* x, cudaStream_t st) {
+    (void)st;
+    drop();
+    GBPC_CUDA_TRY(cudaGraphCreate(&graph, 0));
+    GBPC_CUDA_TRY(cudaGraphConditionalHandleCreate(&while_h, graph, 0, cudaGraphCondAssignDefault));
+    cudaStream_t cs;
+    GBPC_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    int rc = GBPC_OK;
+    cudaGraph_t g2 = nullptr;
+    do {
+      if (cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      rc = record_init(b, x, cs);
+      cudaError_t e = cudaStreamEndCapture(cs, &g2);
+      if (rc) break;
+      if (e != cudaSuccess) {
+        gbpc_set_error_cuda(e, "capture GMRES init", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      cudaGraphNode_t tail = nullptr;
+      tail_of(graph, &tail);
+      cudaGraphNodeParams wp = {};
+      wp.type = cudaGraphNodeTypeConditional;
+      wp.conditional.handle = while_h;
+      wp.conditional.type = cudaGraphCondTypeWhile;
+      wp.conditional.size = 1;
+      cudaGraphNode_t wnode;
+      e = cudaGraphAddNode(&wnode, graph, tail ? &tail : nullptr, nullptr, tail ? 1 : 0, &wp);
+      if (e != cudaSuccess) {
+        gbpc_set_error_cuda(e, "add GMRES while node", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      cudaGraph_t body = wp.conditional.phGraph_out[0];
+      if ((e = cudaGraphConditionalHandleCreate(&if_h, body, 0, cudaGraphCondAssignDefault)) !=
+          cudaSuccess) {
+        gbpc_set_error_cuda(e, "GMRES if handle", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      {
+        PdlScope scope(true);
+        rc = record_step(cs);
+      }
+      e = cudaStreamEndCapture(cs, &g2);
+      if (rc) break;
+      if (e != cudaSuccess) {
+        gbpc_set_error_cuda(e, "capture GMRES step", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      tail_of(body, &tail);
+      cudaGraphNodeParams ip = {};
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = if_h;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      cudaGraphNode_t inode;
+      e = cudaGraphAddNode(&inode, body, tail ? &tail : nullptr, nullptr, tail ? 1 : 0, &ip);
+      if (e != cudaSuccess) {
+        gbpc_set_error_cuda(e, "add GMRES if node", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      cudaGraph_t ibody = ip.conditional.phGraph_out[0];
+      if (cudaStreamBeginCaptureToGraph(cs, ibody, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      rc = record_cycle_end(b, x, cs);
+      e = cudaStreamEndCapture(cs, &g2);
+      if (rc) break;
+      if (e != cudaSuccess) {
+        gbpc_set_error_cuda(e, "capture GMRES cycle end", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      if (e != cudaSuccess) {
+        gbpc_set_error_cuda(e, "instantiate GMRES", __FILE__, __LINE__);
+        rc = GBPC_ERR_CUDA;
+        break;
+      }
+    } while (0);
+    cudaStreamDestroy(cs);
+    if (rc) {
+      drop();
+      cudaGetLastError();
+      return rc;
+    }
+    last_b = b;
+    last_x = x;
+    return GBPC_OK;
+  }
+
+  int run(const double* b, double* x, double tol, double atol, int maxiter, bool use_graph,
+          int32_t* nit, double* res, double* target, cudaStream_t st) {
+    if (maxiter <= 0) maxiter = (int)std::min<int64_t>(std::max<int64_t>(n, 1), 0x7fffffff);
+    int rc;
+    if (use_graph) {
+      if (!exec || last_b != b || last_x != x) {
+        if ((rc = build_graph(b, x, st))) return rc;
+      }
+      gm_setup_kernel<<<1, 1, 0, st>>>(S(), m, tol, atol, maxiter, (unsigned long long)while_h,
+                                       (unsigned long long)if_h);
+      GBPC_CUDA_TRY(cudaGetLastError());
+      GBPC_CUDA_TRY(cudaGraphLaunch(exec, st));
+    } else {
+      // Host-driven loop of the same kernels (every kernel checks the flags).
+      gm_setup_kernel<<<1, 1, 0, st>>>(S(), m, tol, atol, maxiter, 0ull, 0ull);
+      if ((rc = record_init(b, x, st))) return rc;
+      int flags[2] = {1, 0};  // not_done, restart
+      for (int step = 0; step < maxiter + 1 && flags[0]; ++step) {
+        if ((rc = record_step(st))) return rc;
+        GBPC_CUDA_TRY(cudaMemcpyAsync(flags + 1, &S()->restart, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+        if (flags[1] && (rc = record_cycle_end(b, x, st))) return rc;
+        GBPC_CUDA_TRY(cudaMemcpyAsync(flags, &S()->not_done, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+      }
+    }
+    gm_outputs_kernel<<<1, 1, 0, st>>>(S(), nit, res, target);
+    GBPC_CUDA_TRY(cudaGetLastError());
+    return GBPC_OK;
+  }
+};
+
+}  // namespace gbpc
+
+using namespace gbpc;
+
+struct gbpc_gmres {
+  Gmres g;
+};
+
+extern "C" int gbpc_gmres_create(gbpc_op* A, gbpc_op* M, int restart, void* stream,
+                                 gbpc_gmres** out) {
+  if (!out || !A || !A->impl || restart < 1 || restart > kGMaxK - 1) {
+    gbpc_set_error("gbpc_gmres_create: bad arguments (restart must be 1..%d)", kGMaxK - 1);
+    return GBPC_ERR_ARG;
+  }
+  Operator* a = A->impl.get();
+  Operator* m = (M && M->impl) ? M->impl.get() : nullptr;
+  if (a->vdtype != GBPC_F64 || (m && m->vdtype != GBPC_F64)) {
+    gbpc_set_error("GMRES runs on float64 vectors");
+    return GBPC_ERR_ARG;
+  }
+  if (m && m->rows != a->rows) {
+    gbpc_set_error("operator and preconditioner sizes differ (%lld vs %lld)", (long long)a->rows,
+                   (long long)m->rows);
+    return GBPC_ERR_ARG;
+  }
+  auto* h = new gbpc_gmres;
+  Gmres& g = h->g;
+  ByteTally tally(&g.device_bytes);
+  g.A = a;
+  g.M = m;
+  g.n = a->rows;
+  g.m = restart;
+  const size_t vec = sizeof(double) * std::max<int64_t>(g.n, 1);
+  int rc = g.V.alloc(vec * (restart + 1));
+  if (!rc) rc = g.w.alloc(vec);
+  if (!rc) rc = g.t.alloc(vec);
+  if (!rc) rc = g.d.alloc(vec);
+  if (!rc) rc = g.vcur.alloc(vec);
+  if (!rc) rc = g.state.alloc(sizeof(GmresState));
+  if (!rc) rc = g.work.alloc(sizeof(double) * Gmres::work_doubles(restart));
+  if (!rc) rc = g.partials.alloc(sizeof(double) * (size_t)kGCtas * kGMaxK);
+  if (!rc) rc = g.counter.alloc(sizeof(unsigned int));
+  if (!rc) rc = g.rb.init((cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!rc && (cudaMemsetAsync(g.counter.p, 0, sizeof(unsigned int), st) != cudaSuccess ||
+              cudaMemsetAsync(g.work.p, 0, sizeof(double) * Gmres::work_doubles(restart), st) !=
+                  cudaSuccess ||
+              cudaMemsetAsync(g.state.p, 0, sizeof(GmresState), st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess))
+    rc = GBPC_ERR_CUDA;
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_gmres_run(gbpc_gmres* h, const double* b, double* x, double tol, double atol,
+                              int maxiter, int use_graph, int32_t* nit_dev, double* res_dev,
+                              double* target_dev, void* stream) {
+  if (!h || !b || !x) {
+    gbpc_set_error("gbpc_gmres_run: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  return h->g.run(b, x, tol, atol, maxiter, use_graph != 0, nit_dev, res_dev, target_dev,
+                  (cudaStream_t)stream);
+}
+
+extern "C" int gbpc_gmres_device_bytes(const gbpc_gmres* h, size_t* bytes_host) {
+  if (!h || !bytes_host) {
+    gbpc_set_error("gbpc_gmres_device_bytes: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *bytes_host = h->g.device_bytes;
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_gmres_destroy(gbpc_gmres* h) {
+  if (!h) return GBPC_OK;
+  cudaDeviceSynchronize();
+  delete h;
+  return GBPC_OK;
+}

@@ -3,9 +3,10 @@
 Mirrors the parts of ``warp.optim.linear`` that the reference uses: the
 ``LinearOperator(shape, dtype, device, matvec)`` base with
 ``matvec(x, y, z, alpha, beta)`` computing ``z = alpha * Op x + beta * y``,
-``aslinearoperator``, ``preconditioner(A, "diag")`` and ``cg`` / ``cr`` with
-the same signature and return values (device arrays when ``check_every=0``).
-The loops themselves run in libgbpc (one CUDA graph per solve).
+``aslinearoperator``, ``preconditioner(A, "diag")`` and ``cg`` / ``cr`` /
+``gmres`` with the same signatures and return values (device arrays when
+``check_every=0``).  The loops themselves run in libgbpc (one CUDA graph per
+solve).
 """
 
 from __future__ import annotations
@@ -158,3 +159,67 @@ def cr(A, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_eve
        use_cuda_graph=True):
     """Preconditioned conjugate residual (warp.optim.linear.cr signature)."""
     return _solve("cr", A, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+
+
+class GmresSolver:
+    """Reusable restarted GMRES bound to (A, M); repeated runs replay one graph."""
+
+    def __init__(self, A, M=None, restart=31, use_cuda_graph=True):
+        if isinstance(restart, bool) or not isinstance(restart, int) or not 1 <= restart <= 64:
+            raise ValueError("restart must be an integer in [1, 64]")
+        self.A = aslinearoperator(A)
+        self.M = aslinearoperator(M)
+        self.restart = restart
+        self.use_graph = bool(use_cuda_graph)
+        out = ctypes.c_void_p()
+        _lib.call("gbpc_gmres_create", _handle(self.A), _handle(self.M), restart,
+                  _lib.stream(self.A.device), ctypes.byref(out))
+        self._h = out
+        dev = self.A.device
+        self.nit = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.res = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.target = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbpc_gmres_destroy(h)
+            except Exception:
+                pass
+
+    @property
+    def device_bytes(self) -> int:
+        return _lib.object_bytes("gbpc_gmres_device_bytes", self._h)
+
+    def run(self, b, x, tol=None, atol=None, maxiter=0):
+        tol = 1.0e-5 if tol is None else float(tol)
+        atol = 0.0 if atol is None else float(atol)
+        _lib.call("gbpc_gmres_run", self._h, _lib.ptr(_flat(b)), _lib.ptr(_flat(x)), tol, atol,
+                  int(maxiter), int(self.use_graph), _lib.ptr(self.nit), _lib.ptr(self.res),
+                  _lib.ptr(self.target), _lib.stream(self.A.device))
+        return self.nit, self.res, self.target
+
+
+def gmres(A, b, x, tol=None, atol=None, restart=31, maxiter=0, M=None, callback=None,
+          check_every=31, use_cuda_graph=True, is_left_preconditioner=False):
+    """Restarted GMRES (warp.optim.linear.gmres signature), right-preconditioned.
+
+    Returns (steps, residual norm, target) -- device arrays when
+    ``check_every=0``, host numbers otherwise.  The residual norm is
+    ``|b - A x|`` as tracked by the Givens recurrence; the loop stops when it
+    is at most ``max(atol, tol |b|)`` or after ``maxiter`` Arnoldi steps.
+    """
+    if callback is not None:
+        raise NotImplementedError("per-iteration callbacks are not supported; the loop runs on "
+                                  "the device")
+    if is_left_preconditioner:
+        raise NotImplementedError("only right preconditioning is implemented")
+    if b.dtype != torch.float64 or x.dtype != torch.float64:
+        raise TypeError("gmres runs on float64 vectors")
+    s = GmresSolver(A, M, restart, use_cuda_graph)
+    nit, res, target = s.run(b, x, tol, atol, maxiter)
+    if check_every == 0:
+        return nit.clone(), res.clone(), target.clone()
+    vals = torch.stack([nit.to(torch.float64), res, target]).cpu()
+    return int(vals[0]), float(vals[1]), float(vals[2])
