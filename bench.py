@@ -390,6 +390,7 @@ def main():
     if not args.no_mixed:
         line["mixed_batched"] = run_mixed_batched(args, prob, Q, K, mass, free, dev)
     line["refit"] = measure_refit(args, prob, Q, dev)
+    line["assembly"] = measure_assembly(prob, dev)
     if args.lifted:
         line["lifted_gmres"] = measure_lifted_gmres(args, prob, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -548,6 +549,37 @@ def measure_refit(args, prob, Q, dev):
     refit_ms = timed(refit)
     return {"matrix": f"Q with alpha {ALPHA:g} -> {2 * ALPHA:g} (same pattern)",
             "setup_ms": setup_ms, "refit_ms": refit_ms, "setup_over_refit": setup_ms / refit_ms}
+
+
+def measure_assembly(prob, dev):
+    """Q = alpha M + K M^-1 K: the reference's host SciPy product (the
+    workload's untimed assembly) against sparse.spgemm on the device (same
+    summation order; CUDA-event median of 3, inputs resident)."""
+    import torch
+
+    from warp_preconditioners_gb300 import from_scipy, problems, sparse
+
+    t = time.perf_counter()
+    host = problems.biharmonic(prob["K"], prob["mass"], ALPHA)
+    host_ms = (time.perf_counter() - t) * 1e3
+    K = from_scipy(prob["K"], dev)
+    m = torch.as_tensor(prob["mass"], device=dev)
+    d, e = 1.0 / m, ALPHA * m
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        Q = sparse.spgemm(K, K, col_scale=d, add_diag=e)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    vals = Q.values.cpu().numpy()
+    same = (Q.nnz == host.nnz and np.array_equal(Q.columns.cpu().numpy(), host.indices))
+    return {"host_scipy_ms": host_ms, "device_ms": statistics.median(times), "nnz": Q.nnz,
+            "same_pattern": bool(same),
+            "max_rel_diff": float(np.max(np.abs(vals - host.data) / np.abs(host.data)))
+            if same else None}
 
 
 def measure_lifted_gmres(args, prob, dev, restart=31, maxiter=30000):

@@ -130,6 +130,18 @@ int gbpc_fsai_refit(int n, const int32_t* a_off, const int32_t* a_col, const voi
                     double pivot_floor, void* out, int factor_dtype, int32_t* status_host,
                     void* stream);
 
+/* C = A diag(col_scale) B + diag(add_diag), float64 scalar CSR (col_scale,
+ * add_diag nullable), on the device: the host SciPy assembly of the
+ * smoothing operator Q = alpha M + K M^-1 K (results/dirichlet-tuning/
+ * README.md:72-77) with the same summation order (contributions to C_ik in
+ * increasing j, then the diagonal term), exact zeros dropped, rows sorted.
+ * Two-phase like gbpc_fsai_pack: c_col == NULL fills c_off[nrow+1] and
+ * *nnz_host; the second call writes c_col / c_val.  Synchronises. */
+int gbpc_spgemm(int nrow, int ncol, const int32_t* a_off, const int32_t* a_col,
+                const double* a_val, const double* col_scale, int b_nrow, const int32_t* b_off,
+                const int32_t* b_col, const double* b_val, const double* add_diag, int32_t* c_off,
+                int32_t* c_col, double* c_val, int64_t* nnz_host, void* stream);
+
 /* map_out[e] = position in the transpose (t_offsets/t_columns) of entry e of
  * the CSR matrix: replaces fsai_reuse.py `transpose_map` (:54-63).
  * GBPC_ERR_ARG if an entry has no transposed counterpart.  Synchronises. */
@@ -156,6 +168,18 @@ typedef struct gbpc_op gbpc_op;
 int gbpc_op_sparse(int nrow, int ncol, int block, const int32_t* offsets,
                    const int32_t* columns, const void* values, int value_dtype,
                    int vector_dtype, void* stream, gbpc_op** out);
+
+/* Preconditioners of the mixed harmonic systems (vectors interleave `order`
+ * = 2 or 3 unknowns per vertex, n vertices; K scalar CSR, mass[n], both in
+ * `dtype`; hinv an operator of this library approximating H^-1 on n-vectors,
+ * referenced, not owned).  MatchingSchur replaces mixed.py:283-334 (block
+ * elimination with repeated H^-1), ShiftedBlock mixed.py:388-427 (scale =
+ * data_weight^(1/4)). */
+int gbpc_op_matching_schur(int order, int n, const int32_t* k_off, const int32_t* k_col,
+                           const void* k_val, int dtype, const void* mass, gbpc_op* hinv,
+                           void* stream, gbpc_op** out);
+int gbpc_op_shifted_block(int order, int n, double scale, int dtype, gbpc_op* hinv, void* stream,
+                          gbpc_op** out);
 
 /* Gram-form approximate inverse z = alpha * G^T (G x) + beta * y from
  * explicit G and G^T (scalar CSR, or b x b BSR for block FSAI).  Replaces

@@ -977,6 +977,67 @@ int32_t fsai_refit(int n, const int32_t* off, const int32_t* col, const T* val, 
 
 }  // namespace
 
+namespace {
+
+// SciPy's csr_matmat (scipy/sparse/sparsetools/csr.h) as used by the
+// reference's host assembly K @ diags(d) @ K + diags(e).  csr_matmat emits
+// each row in reverse insertion order (a linked list of touched columns), so
+// the intermediate K diags(d) holds row i in decreasing column order and the
+// second product accumulates the contributions A_ij d_j B_jk into C_ik over
+// j DEcreasing, from zero (without d, A @ B walks sorted A rows: j
+// increasing); then e_i is added to the diagonal; exact zeros are dropped
+// and rows sorted.
+// Returns nnz; with c_col == nullptr only c_off is filled.
+int64_t spgemm(int nrow, int ncol, const int32_t* a_off, const int32_t* a_col, const double* a_val,
+               const double* d, const int32_t* b_off, const int32_t* b_col, const double* b_val,
+               const double* e, int32_t* c_off, int32_t* c_col, double* c_val) {
+  std::vector<double> sums(ncol, 0.0);
+  std::vector<char> used(ncol, 0);
+  std::vector<int> cols;
+  int64_t nnz = 0;
+  c_off[0] = 0;
+  for (int i = 0; i < nrow; ++i) {
+    cols.clear();
+    const int len = a_off[i + 1] - a_off[i];
+    for (int t = 0; t < len; ++t) {
+      const int jj = d ? a_off[i + 1] - 1 - t : a_off[i] + t;
+      const int j = a_col[jj];
+      const double v = d ? a_val[jj] * d[j] : a_val[jj];
+      for (int kk = b_off[j]; kk < b_off[j + 1]; ++kk) {
+        const int k = b_col[kk];
+        if (!used[k]) {
+          used[k] = 1;
+          cols.push_back(k);
+        }
+        sums[k] += v * b_val[kk];
+      }
+    }
+    if (e) {
+      if (!used[i]) {
+        used[i] = 1;
+        cols.push_back(i);
+      }
+      sums[i] += e[i];
+    }
+    std::sort(cols.begin(), cols.end());
+    for (int k : cols) {
+      if (sums[k] != 0.0) {
+        if (c_col) {
+          c_col[nnz] = k;
+          c_val[nnz] = sums[k];
+        }
+        ++nnz;
+      }
+      sums[k] = 0.0;
+      used[k] = 0;
+    }
+    c_off[i + 1] = (int32_t)nnz;
+  }
+  return nnz;
+}
+
+}  // namespace
+
 extern "C" {
 
 int or_num_threads() {
@@ -1213,5 +1274,11 @@ int32_t or_fsai_refit_f32_f32(int n, const int32_t* off, const int32_t* col, con
                               const float* scale, const int32_t* goff, const int32_t* gcol,
                               float floor_, float* out) {
   return fsai_refit<float, float>(n, off, col, val, scale, goff, gcol, floor_, out);
+}
+int64_t or_spgemm(int nrow, int ncol, const int32_t* a_off, const int32_t* a_col,
+                  const double* a_val, const double* d, const int32_t* b_off,
+                  const int32_t* b_col, const double* b_val, const double* e, int32_t* c_off,
+                  int32_t* c_col, double* c_val) {
+  return spgemm(nrow, ncol, a_off, a_col, a_val, d, b_off, b_col, b_val, e, c_off, c_col, c_val);
 }
 }  // extern "C"

@@ -195,6 +195,23 @@ def fsai_refit(a: CSR, g: CSR, pivot_floor=None, factor_dtype=None):
     return out[:len(g.columns)], int(status[0]), int(bad)
 
 
+def spgemm(a: CSR, b: CSR, col_scale=None, add_diag=None) -> CSR:
+    """SciPy's order for A @ diags(d) @ B + diags(e) (the reference's host
+    assembly of Q: inner index decreasing), separately rounded; sorted CSR."""
+    fn = lib().or_spgemm
+    fn.restype = ctypes.c_int64
+    d = None if col_scale is None else np.ascontiguousarray(col_scale, np.float64)
+    e = None if add_diag is None else np.ascontiguousarray(add_diag, np.float64)
+    off = np.empty(a.nrow + 1, np.int32)
+    args = [a.nrow, b.ncol, _p(a.offsets), _p(a.columns), _p(a.values), _p(d), _p(b.offsets),
+            _p(b.columns), _p(b.values), _p(e), _p(off)]
+    nnz = fn(*args, None, None)
+    col = np.empty(max(nnz, 1), np.int32)
+    val = np.empty(max(nnz, 1))
+    fn(*args, _p(col), _p(val))
+    return CSR(off, col[:nnz], val[:nnz], b.ncol)
+
+
 def csr_spmv(a: CSR, x, y, alpha, beta, accum_dtype=None):
     accum_dtype = np.dtype(accum_dtype or a.values.dtype)
     x = np.ascontiguousarray(x, accum_dtype)

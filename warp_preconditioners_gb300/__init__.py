@@ -5,7 +5,8 @@ arguments and error messages), backed by hand-written sm_103a CUDA kernels in
 libgbpc.so reached through its C ABI (include/gbpc.h):
 
     FSAI, SparseOperator, SquaredLaplacianOperator, BlockJacobi, BlockILU0,
-    BiharmonicSystem, RepeatedFSAI, BlockFSAI, BsrBlockFSAI
+    BiharmonicSystem, RepeatedFSAI, BlockFSAI, BsrBlockFSAI, MixedHarmonicSystem,
+    MatchingSchur, ShiftedBlock
 
 plus ``linear.cg`` / ``linear.cr`` / ``linear.gmres`` / ``linear.preconditioner`` and the
 ``sparse`` helpers that stand in for warp.optim.linear and warp.sparse.
@@ -18,6 +19,7 @@ from .block_fsai import BlockFSAI, BsrBlockFSAI
 from .block_ilu import BlockILU0, BlockJacobi
 from .fsai import FSAI
 from .linear import LinearOperator, aslinearoperator, cg, cr, gmres, preconditioner
+from .mixed import MatchingSchur, MixedHarmonicSystem, ShiftedBlock
 from .sparse import BsrMatrix, bsr_copy, bsr_from_triplets, bsr_transposed, from_scipy
 from .sparse_operator import SparseOperator
 from .squared_laplacian import SquaredLaplacianOperator
@@ -32,6 +34,9 @@ __all__ = [
     "BlockILU0",
     "BlockFSAI",
     "BsrBlockFSAI",
+    "MixedHarmonicSystem",
+    "MatchingSchur",
+    "ShiftedBlock",
     "LinearOperator",
     "BsrMatrix",
     "aslinearoperator",

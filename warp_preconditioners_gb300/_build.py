@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # Translation units whose arithmetic must follow the reference operation by
 # operation (no multiply-add contraction).
-EXACT = {"gbpc_fsai.cu", "gbpc_block.cu"}
+EXACT = {"gbpc_fsai.cu", "gbpc_block.cu", "gbpc_spgemm.cu"}
 
 
 def _nvcc() -> str:

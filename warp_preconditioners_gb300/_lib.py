@@ -58,6 +58,8 @@ _SIGNATURES = {
     "gbpc_convert_factor": [_int, _vp, _vp, _vp, _int, _vp, _int, _i32p, _vp],
     "gbpc_fsai_refit": [_int, _vp, _vp, _vp, _int, _vp, _vp, _int, _dbl, _vp, _int, _i32p, _vp],
     "gbpc_transpose_map": [_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gbpc_spgemm": [_int, _int, _vp, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                    _i64p, _vp],
     "gbpc_scatter_values": [ctypes.c_int64, _vp, _vp, _vp, _int, _vp],
     "gbpc_op_fsai_refill": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _vp],
     "gbpc_op_sparse": [_int, _int, _int, _vp, _vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
@@ -68,6 +70,9 @@ _SIGNATURES = {
     "gbpc_op_diagonal": [_int, _int, _vp, _vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_op_block_jacobi": [_int, _int, _vp, _vp, _vp, _int, _dbl, _vp, _vp, ctypes.POINTER(_vp)],
     "gbpc_op_block_jacobi_update": [_vp, _int, _int, _vp, _vp, _vp, _int, _dbl, _vp, _vp],
+    "gbpc_op_matching_schur": [_int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp,
+                               ctypes.POINTER(_vp)],
+    "gbpc_op_shifted_block": [_int, _int, _dbl, _int, _vp, _vp, ctypes.POINTER(_vp)],
     "gbpc_op_bilu0": [_int, _int, _vp, _vp, _vp, _int, _int, _int, _dbl, _dbl, _vp, _vp, _vp,
                       ctypes.POINTER(_vp)],
     "gbpc_block_fsai_setup": [_int, _int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp],

@@ -14,7 +14,7 @@
 // conditional while-node whose body is one Arnoldi step followed by a
 // conditional if-node holding the end-of-cycle update (back-substitution,
 // solution update, new residual).  Every reduction is deterministic: per-CTA
-// partials combined in index order by the last CTA to finish.
+// partials, combined in a fixed order by a warp of the last CTA to finish.
 
 #include <algorithm>
 #include <cmath>
@@ -72,6 +72,19 @@ __device__ __forceinline__ double cta_sum(double v, double* sm) {
   return s;
 }
 
+// Total of count partials (stride apart) by one warp: lane l adds the
+// partials l, l+32, ... in order, then a fixed shuffle tree (every lane
+// returns the total).  Deterministic and short: the partials are loaded in
+// parallel instead of one dependent load after another.
+__device__ __forceinline__ double warp_total(const double* p, unsigned count, size_t stride) {
+  const int lane = threadIdx.x & 31;
+  double t = 0.0;
+  for (unsigned c = lane; c < count; c += 32) t += __ldcg(p + (size_t)c * stride);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;
+}
+
 // Last CTA to arrive gets true (after its partial is visible).
 __device__ __forceinline__ bool arrive_last(unsigned int* counter) {
   __shared__ bool last;
@@ -110,13 +123,14 @@ gm_bnorm_kernel(int64_t n, const double* b, GmresState* s, double* partials,
     acc = fma(b[r], b[r], acc);
   const double cs = cta_sum(acc, sm);
   if (threadIdx.x == 0) partials[blockIdx.x] = cs;
-  if (arrive_last(counter) && threadIdx.x == 0) {
-    double t = 0.0;
-    for (unsigned c = 0; c < gridDim.x; ++c) t += __ldcg(partials + c);
-    s->bb = t;
-    const double a = fmax(s->atol, s->tol * sqrt(t));
-    s->atol_sq = a * a;
-    *counter = 0u;
+  if (arrive_last(counter) && threadIdx.x < 32) {
+    const double t = warp_total(partials, gridDim.x, 1);
+    if (threadIdx.x == 0) {
+      s->bb = t;
+      const double a = fmax(s->atol, s->tol * sqrt(t));
+      s->atol_sq = a * a;
+      *counter = 0u;
+    }
   }
 }
 
@@ -146,11 +160,12 @@ gm_mdot_kernel(int64_t n, const double* V, const double* w, GmresState* s, Gmres
     partials[(size_t)blockIdx.x * kGMaxK + threadIdx.x] = t;
   }
   if (arrive_last(counter)) {
-    if (threadIdx.x < k) {
-      double t = 0.0;
-      for (unsigned c = 0; c < gridDim.x; ++c) t += __ldcg(partials + (size_t)c * kGMaxK + threadIdx.x);
-      wk.coef[threadIdx.x] = t;
-      wk.hcol[threadIdx.x] = accumulate ? wk.hcol[threadIdx.x] + t : t;
+    for (int i = warp; i < k; i += kGT / 32) {  // warp w: coefficients w, w+8, ...
+      const double t = warp_total(partials + i, gridDim.x, kGMaxK);
+      if (lane == 0) {
+        wk.coef[i] = t;
+        wk.hcol[i] = accumulate ? wk.hcol[i] + t : t;
+      }
     }
     if (threadIdx.x == 0) *counter = 0u;
   }
@@ -225,12 +240,13 @@ gm_update_kernel(int64_t n, const double* V, double* w, GmresState* s, GmresWork
   if (!norm) return;
   const double c = cta_sum(acc, sm);
   if (threadIdx.x == 0) partials[blockIdx.x] = c;
-  if (arrive_last(counter) && threadIdx.x == 0) {
-    double t = 0.0;
-    for (unsigned q = 0; q < gridDim.x; ++q) t += __ldcg(partials + q);
-    s->ww = t;
-    gm_step_finalize(s, wk, t);
-    *counter = 0u;
+  if (arrive_last(counter) && threadIdx.x < 32) {
+    const double t = warp_total(partials, gridDim.x, 1);
+    if (threadIdx.x == 0) {
+      s->ww = t;
+      gm_step_finalize(s, wk, t);
+      *counter = 0u;
+    }
   }
 }
 

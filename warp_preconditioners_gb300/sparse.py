@@ -222,3 +222,40 @@ def bsr_mv(a: BsrMatrix, x, y, alpha=1.0, beta=0.0):
 
     aslinearoperator(a).matvec(x, y, y, alpha, beta)
     return y
+
+
+def spgemm(A: BsrMatrix, B: BsrMatrix, col_scale=None, add_diag=None) -> BsrMatrix:
+    """``A diag(col_scale) B + diag(add_diag)`` on the device (float64 scalar
+    CSR): the host SciPy assembly ``A @ diags(d) @ B + diags(e)`` with the
+    same summation order (over the inner index downwards, as SciPy's
+    intermediate ``A @ diags(d)`` stores its rows), exact zeros dropped and
+    rows sorted."""
+    import ctypes
+
+    from . import _lib
+
+    for m in (A, B):
+        if m.block_shape != (1, 1) or m.scalar_type != torch.float64:
+            raise ValueError("spgemm takes float64 scalar CSR matrices")
+    if A.ncol != B.nrow:
+        raise ValueError("inner dimensions differ")
+    dev = A.device
+    if col_scale is not None and (col_scale.dtype != torch.float64 or col_scale.numel() != A.ncol):
+        raise ValueError("col_scale must be float64 with one entry per column of A")
+    if add_diag is not None and (add_diag.dtype != torch.float64 or add_diag.numel() != A.nrow
+                                 or A.nrow > B.ncol):
+        raise ValueError("add_diag must be float64 with one entry per row")
+    d = col_scale.contiguous() if col_scale is not None else None
+    e = add_diag.contiguous() if add_diag is not None else None
+    off = torch.empty(A.nrow + 1, dtype=torch.int32, device=dev)
+    nnz = ctypes.c_int64()
+    args = [A.nrow, B.ncol, _lib.ptr(A.offsets), _lib.ptr(A.columns), _lib.ptr(A.values),
+            _lib.ptr(d) if d is not None else None, B.nrow, _lib.ptr(B.offsets),
+            _lib.ptr(B.columns), _lib.ptr(B.values), _lib.ptr(e) if e is not None else None,
+            _lib.ptr(off)]
+    _lib.call("gbpc_spgemm", *args, None, None, ctypes.byref(nnz), _lib.stream(dev))
+    col = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
+    val = torch.empty(max(nnz.value, 1), dtype=torch.float64, device=dev)
+    _lib.call("gbpc_spgemm", *args, _lib.ptr(col), _lib.ptr(val), ctypes.byref(nnz),
+              _lib.stream(dev))
+    return BsrMatrix(A.nrow, B.ncol, (1, 1), off, col[:nnz.value], val[:nnz.value])
