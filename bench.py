@@ -77,6 +77,9 @@ def parse_args():
                    help="skip the one-at-a-time float64 arm")
     p.add_argument("--no-mixed", action="store_true",
                    help="skip the mixed-precision 32-RHS batched measurement")
+    p.add_argument("--fp32-refinement", action="store_true",
+                   help="also run float32 inner solves with float64 refinement on the 32 RHS "
+                        "(does not reach float64 accuracy at 70^3; about a minute)")
     p.add_argument("--lifted", action="store_true",
                    help="also time the lifted first-order system under GMRES (the "
                         "reference's lifted-gmres method) on the first right-hand side")
@@ -389,6 +392,8 @@ def main():
         line["e2e"] = run_e2e(args, prob, dev, one_step, world, dist)
     if not args.no_mixed:
         line["mixed_batched"] = run_mixed_batched(args, prob, Q, K, mass, free, dev)
+    if not args.no_mixed:
+        line["batched_rhs4"] = measure_batched_rhs4(args, prob, Q, K, mass, dev, ms_per_step)
     line["refit"] = measure_refit(args, prob, Q, dev)
     line["assembly"] = measure_assembly(prob, dev)
     if args.lifted:
@@ -478,7 +483,8 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
     batch64()  # warm-up (graph capture paths)
     t_plain, (xs, its) = timed(plain)
     t_batch, (Xb, nitb) = timed(batch64)
-    t_mixed, (Xm, outer, inner) = timed(mixed)
+    if args.fp32_refinement:
+        t_mixed, (Xm, outer, inner) = timed(mixed)
     qh = prob["Q"]
     absq = abs(qh)
     x_p = xs.cpu().numpy().T
@@ -493,8 +499,7 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
 
     berr_p, _ = quality(x_p)
     berr_b, rel_b = quality(Xb.cpu().numpy())
-    berr_m, rel_m = quality(Xm.cpu().numpy())
-    return {
+    out = {
         "workload": f"{k} seeded U[-1,1] RHS of the {args.side}^3 smoothing system; setup + solve",
         "plain_fp64_sequential_ms": t_plain, "plain_solves_per_s": k / (t_plain / 1e3),
         "plain_iterations_max": int(max(int(i.item()) for i in its)),
@@ -505,13 +510,16 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             "ms": t_batch, "solves_per_s": k / (t_batch / 1e3), "speedup": t_plain / t_batch,
             "iterations_max": int(nitb.max().item()), "backward_error_max": berr_b,
             "rel_diff_vs_plain_max": rel_b},
-        "float32_refinement": {
+    }
+    if args.fp32_refinement:
+        berr_m, rel_m = quality(Xm.cpu().numpy())
+        out["float32_refinement"] = {
             "solver": "inner float32 PCG (float32 factored operator, bfloat16 FSAI, float64 "
                       "dots), float64 refinement, 8 outer steps max",
             "ms": t_mixed, "speedup": t_plain / t_mixed, "outer_max": int(max(outer)),
             "inner_max": int(max(inner)), "backward_error_max": berr_m,
-            "rel_diff_vs_plain_max": rel_m},
-    }
+            "rel_diff_vs_plain_max": rel_m}
+    return out
 
 
 def measure_refit(args, prob, Q, dev):
@@ -549,6 +557,46 @@ def measure_refit(args, prob, Q, dev):
     refit_ms = timed(refit)
     return {"matrix": f"Q with alpha {ALPHA:g} -> {2 * ALPHA:g} (same pattern)",
             "setup_ms": setup_ms, "refit_ms": refit_ms, "setup_over_refit": setup_ms / refit_ms}
+
+
+def measure_batched_rhs4(args, prob, Q, K, mass, dev, ms_per_step):
+    """The same step (setup + the four right-hand sides) with the four solved
+    together by the batched float64 PCG (rows packed 8 per warp, 4 lanes per
+    row; matrix bytes read once per iteration for all four), against the
+    drop-in one-at-a-time step timed above.  CUDA events, median of 3."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, batched
+
+    B = torch.as_tensor(prob["rhs"].T.copy(), device=dev).contiguous()  # [n, 4]
+    X = torch.zeros_like(B)
+
+    def step():
+        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+        bs = batched.BatchedSolver(K, mass, ALPHA, pre)
+        X.zero_()
+        return bs.solve(B, X, tol=args.rtol, maxiter=100000)
+
+    step()
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        nit, _ = step()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    t = statistics.median(times)
+    qh = prob["Q"]
+    x = X.cpu().numpy()
+    berr = max(float(np.max(np.abs(prob["rhs"][k] - qh @ x[:, k])
+                            / (abs(qh) @ np.abs(x[:, k]) + np.abs(prob["rhs"][k]))))
+               for k in range(4))
+    return {"solver": "one batched float64 PCG for the 4 right-hand sides (FSAI w8)",
+            "ms_per_step": t, "solves_per_s": 4000.0 / t,
+            "speedup_vs_drop_in": ms_per_step / t,
+            "iterations": [int(i) for i in nit.cpu()], "backward_error_max": berr}
 
 
 def measure_assembly(prob, dev):
