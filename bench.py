@@ -62,10 +62,14 @@ def parse_args():
                    help="CG iterations per right-hand side in the CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--config", choices=["c2", "c3", "c5"], default="c2",
+    p.add_argument("--config", choices=["c2", "c2sweep", "c3", "c5", "gmres"], default="c2",
                    help="c2: biharmonic smoothing (default); c3: K (x) C block coupling, "
                         "every preconditioner under CG and CR; c5: serving stream")
     p.add_argument("--c3-grid", type=int, default=64)
+    p.add_argument("--gmres-steps", type=int, default=300,
+                   help="--config gmres: Arnoldi steps timed")
+    p.add_argument("--host-loop", action="store_true",
+                   help="--config gmres: host-driven loop instead of the graph (for ncu)")
     p.add_argument("--c5-requests", type=int, default=200,
                    help="requests replayed from the seed-0 stream (its first N of 2,000)")
     p.add_argument("--c5-rate", type=float, default=4.0, help="Poisson arrivals per second")
@@ -265,6 +269,14 @@ def main():
     if args.config == "c5":
         if rank == 0:
             print(json.dumps(run_c5(args, torch.device("cuda", local))), flush=True)
+        return
+    if args.config == "gmres":
+        if rank == 0:
+            print(json.dumps(run_gmres_steps(args, torch.device("cuda", local))), flush=True)
+        return
+    if args.config == "c2sweep":
+        if rank == 0:
+            print(json.dumps(run_c2_sweep(args, torch.device("cuda", local))), flush=True)
         return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -678,6 +690,103 @@ def measure_lifted_gmres(args, prob, dev, restart=31, maxiter=30000):
             "setup_ms": e0.elapsed_time(e1), "solve_ms": e2.elapsed_time(e3),
             "iterations": int(nit.item()), "residual": float(res.item()),
             "target": float(target.item()), "backward_error": berr}
+
+
+def run_gmres_steps(args, dev):
+    """Arnoldi-step cost of GMRES(31) on the lifted 2x2-block biharmonic
+    system of the --side tet cube (tau = 1e4, FSAI w8 of H = M + sqrt(tau) K
+    on both components): --gmres-steps steps from x = 0 on a unit right-hand
+    side with an unreachable tolerance, so every step runs."""
+    import torch
+
+    from warp_preconditioners_gb300 import BiharmonicSystem, from_scipy, linear, problems
+
+    torch.cuda.set_device(dev)
+    _, _, K, mass = problems.tet_cube(args.side)
+    system = BiharmonicSystem(from_scipy(K, dev), torch.as_tensor(mass, device=dev), 1e4)
+    pre = system.preconditioner(max_row_size=args.width, kap_tolerance=1e-3)
+    b = system.rhs(torch.ones(K.shape[0], dtype=torch.float64, device=dev))
+    x = torch.zeros_like(b)
+    solver = linear.GmresSolver(system.matrix, pre, restart=31,
+                                use_cuda_graph=not args.host_loop)
+    solver.run(b, x, 1e-14, 0.0, 5)
+    x.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    nit, res, _ = solver.run(b, x, 1e-14, 0.0, args.gmres_steps)
+    e1.record()
+    torch.cuda.synchronize()
+    steps = int(nit.item())
+    return {"config": {"workload": f"lifted biharmonic, {args.side}^3 tet cube "
+                                   f"({2 * K.shape[0]} unknowns), GMRES(31) + FSAI w{args.width}",
+                       "loop": "host" if args.host_loop else "graph"},
+            "metric": "ms per Arnoldi step", "steps": steps,
+            "ms_per_step": e0.elapsed_time(e1) / max(steps, 1)}
+
+
+def run_c2_sweep(args, dev):
+    """The smoothing system's FSAI variants: (width, step) in {8, 48} x {1, 2}
+    with kap 1e-3, and the tuned kap 3e-3 with a float32 factor, under CG and
+    CR; first right-hand side, to the bench tolerance.  Setup (FSAI on Q) and
+    solve are CUDA-event medians of 3; accuracy is the componentwise backward
+    error on Q."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, from_scipy, linear
+
+    torch.cuda.set_device(dev)
+    prob = build_problem(args.side)
+    n = prob["n"]
+    Q = from_scipy(prob["Q"], dev)
+    K = from_scipy(prob["K"], dev)
+    mass = torch.as_tensor(prob["mass"], device=dev)
+    free = torch.arange(n, dtype=torch.int32, device=dev)
+    op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
+    b = torch.as_tensor(prob["rhs"][0], device=dev).contiguous()
+    qh = prob["Q"]
+    absq = abs(qh)
+
+    def ev(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    variants = [(8, 1, 1e-3, None), (8, 2, 1e-3, None), (48, 1, 1e-3, None),
+                (48, 2, 1e-3, None), (8, 1, 3e-3, torch.float32)]
+    rows = {}
+    for w, step, kap, fdt in variants:
+        make = lambda: FSAI(Q, max_row_size=w, max_step_size=step, kap_tolerance=kap,
+                            factor_dtype=fdt)
+        make()
+        setups = []
+        for _ in range(3):
+            t, pre = ev(make)
+            setups.append(t)
+        for method in ("cg", "cr"):
+            solver = linear.Solver(method, op, pre)
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            solver.run(b, x, tol=args.rtol, maxiter=100000)
+            times = []
+            for _ in range(3):
+                x.zero_()
+                t, (nit, rr, at) = ev(lambda: solver.run(b, x, tol=args.rtol, maxiter=100000))
+                times.append(t)
+            u = x.cpu().numpy()
+            rhs = prob["rhs"][0]
+            berr = float(np.max(np.abs(rhs - qh @ u) / (absq @ np.abs(u) + np.abs(rhs))))
+            name = f"w{w}_step{step}_kap{kap:g}" + ("_f32" if fdt is not None else "") + f"/{method}"
+            rows[name] = {"setup_ms": statistics.median(setups),
+                          "solve_ms": statistics.median(times),
+                          "iterations": int(nit.item()), "converged": bool(rr.item() <= at.item()),
+                          "factor_nnz": pre.G.nnz, "backward_error": berr}
+    return {"config": {"workload": f"biharmonic smoothing, {args.side}^3 tet cube, first RHS, "
+                                   f"CG/CR to {args.rtol:g}, FSAI variants"},
+            "metric": "setup + solve ms per FSAI variant and solver", "results": rows}
 
 
 def run_c3(args, dev, maxiter=20000):

@@ -169,8 +169,17 @@ __device__ __forceinline__ void b_reduce(const BRed& red, double v) {
     // warp 0 adds the warp sums in order: deterministic and short.
     __threadfence();
     double s = 0.0;
-    for (unsigned int c = warp; c < gridDim.x; c += kBWarps)
-      s += __ldcg(red.partials + (size_t)c * kB + lane);
+    unsigned int c = warp;
+    // Eight CTA partials loaded together, added in the same order as one at
+    // a time (the sum is unchanged; the loads no longer wait on each other).
+    for (; c + 7 * kBWarps < gridDim.x; c += 8 * kBWarps) {
+      double v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = __ldcg(red.partials + (size_t)(c + q * kBWarps) * kB + lane);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s += v[q];
+    }
+    for (; c < gridDim.x; c += kBWarps) s += __ldcg(red.partials + (size_t)c * kB + lane);
     sm[warp][lane] = s;
     __syncthreads();
     if (warp == 0) {

@@ -14,7 +14,16 @@
 // conditional while-node whose body is one Arnoldi step followed by a
 // conditional if-node holding the end-of-cycle update (back-substitution,
 // solution update, new residual).  Every reduction is deterministic: per-CTA
-// partials, combined in a fixed order by a warp of the last CTA to finish.
+// partials, combined in a fixed order by the last CTA to finish.
+//
+// FP64 throughput, not memory, bounds the Gram-Schmidt kernels on this part
+// (about 1.7 FP64 operations per clock per SM, the same for a warp
+// instruction whatever its active lanes), so their reductions are laid out
+// to spend as few FP64 warp instructions as possible: a reduce-scatter
+// butterfly across the lanes, cluster-level sums through distributed shared
+// memory, and final sums with one coefficient per lane.
+
+#include <cooperative_groups.h>
 
 #include <algorithm>
 #include <cmath>
@@ -30,9 +39,17 @@ int copy_with_dot(int64_t n, const double* x, double* z, const int* guard, const
 
 namespace {
 
+namespace cg = cooperative_groups;
+
 constexpr int kGT = 256;          // threads per CTA
 constexpr int kGMaxK = 65;        // basis vectors (restart <= 64)
 constexpr int kGCtas = 152 * 4;   // CTAs of the vector kernels (at most)
+constexpr int kGChunk = 16;       // basis vectors per pass over the rows
+constexpr int kGCluster = 8;      // CTAs per cluster of the multi-dot
+constexpr int kMdotCtas = 152 * 2;  // multi-dot CTAs (at most; a multiple of kGCluster)
+constexpr int kMdotClusters = kMdotCtas / kGCluster;
+static_assert(kMdotCtas % kGCluster == 0, "multi-dot grid must hold whole clusters");
+static_assert(kMdotClusters <= kGCtas, "multi-dot partials fit the partials buffer");
 
 struct GmresState {
   int m, j, it, maxiter;
@@ -59,6 +76,14 @@ __device__ __forceinline__ void set_cond(unsigned long long h, bool v) {
 
 int g_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kGT - 1) / kGT, kGCtas)); }
 
+// Multi-dot grid: whole clusters, at most two CTAs per SM (fewer partials
+// for the final sum; a thread takes one or two rows).
+int mdot_grid(int64_t n) {
+  int64_t g = (n + kGT - 1) / kGT;
+  g = (g + kGCluster - 1) / kGCluster * kGCluster;
+  return (int)std::max<int64_t>(kGCluster, std::min<int64_t>(g, kMdotCtas));
+}
+
 // Sum of a value over the CTA (kGT threads), valid in thread 0.
 __device__ __forceinline__ double cta_sum(double v, double* sm) {
 #pragma unroll
@@ -72,25 +97,29 @@ __device__ __forceinline__ double cta_sum(double v, double* sm) {
   return s;
 }
 
-// Total of count partials (stride apart) by one warp: lane l adds the
-// partials l, l+32, ... in order, then a fixed shuffle tree (every lane
-// returns the total).  Deterministic and short: the partials are loaded in
-// parallel instead of one dependent load after another.
-__device__ __forceinline__ double warp_total(const double* p, unsigned count, size_t stride) {
-  const int lane = threadIdx.x & 31;
-  double t = 0.0;
-  for (unsigned c = lane; c < count; c += 32) t += __ldcg(p + (size_t)c * stride);
+// Total of count (<= kGCtas) partials by the whole CTA: thread t adds the
+// partials t, t + kGT, ... (every load issued before the adds), then
+// cta_sum.  Deterministic for a given count; valid in thread 0.
+__device__ __forceinline__ double cta_total(const double* p, unsigned count, double* sm) {
+  constexpr int L = (kGCtas + kGT - 1) / kGT;
+  double v[L];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  return t;
+  for (int q = 0; q < L; ++q) {
+    const unsigned c = threadIdx.x + q * kGT;
+    v[q] = c < count ? __ldcg(p + c) : 0.0;
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int q = 0; q < L; ++q) t += v[q];
+  return cta_sum(t, sm);
 }
 
-// Last CTA to arrive gets true (after its partial is visible).
-__device__ __forceinline__ bool arrive_last(unsigned int* counter) {
+// Last of `arrivals` CTAs to arrive gets true (after its partial is visible).
+__device__ __forceinline__ bool arrive_last(unsigned int* counter, unsigned arrivals) {
   __shared__ bool last;
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == arrivals - 1;
   __syncthreads();
   if (last) __threadfence();
   return last;
@@ -123,8 +152,8 @@ gm_bnorm_kernel(int64_t n, const double* b, GmresState* s, double* partials,
     acc = fma(b[r], b[r], acc);
   const double cs = cta_sum(acc, sm);
   if (threadIdx.x == 0) partials[blockIdx.x] = cs;
-  if (arrive_last(counter) && threadIdx.x < 32) {
-    const double t = warp_total(partials, gridDim.x, 1);
+  if (arrive_last(counter, gridDim.x)) {
+    const double t = cta_total(partials, gridDim.x, sm);
     if (threadIdx.x == 0) {
       s->bb = t;
       const double a = fmax(s->atol, s->tol * sqrt(t));
@@ -134,38 +163,139 @@ gm_bnorm_kernel(int64_t n, const double* b, GmresState* s, double* partials,
   }
 }
 
+// Reduce-scatter of C (<= 16) per-lane values across the warp, padded to
+// P = 2^p with zeros: level l trades half of the remaining values with the
+// lane 16 >> l away and adds, so after p levels lane L holds a partial of
+// value L >> (5 - p); 5 - p plain butterfly levels complete it.  P - 1 + 5 - p
+// adds per lane against 5 C for C separate shuffle trees.
+template <int C>
+struct Scatter {
+  static constexpr int P = C <= 1 ? 1 : C <= 2 ? 2 : C <= 4 ? 4 : C <= 8 ? 8 : 16;
+  static constexpr int p = P == 1 ? 0 : P == 2 ? 1 : P == 4 ? 2 : P == 8 ? 3 : 4;
+  static constexpr int low = 5 - p;  // lanes sharing a value: 1 << low
+};
+
+template <int C>
+__device__ __forceinline__ double scatter_sum(const double (&a)[C]) {
+  constexpr int P = Scatter<C>::P, p = Scatter<C>::p;
+  const int lane = threadIdx.x & 31;
+  double v[P];
+#pragma unroll
+  for (int q = 0; q < P; ++q) v[q] = q < C ? a[q] : 0.0;
+#pragma unroll
+  for (int l = 0; l < p; ++l) {
+    const int half = P >> (l + 1), off = 16 >> l;
+    const bool up = (lane & off) != 0;
+#pragma unroll
+    for (int q = 0; q < half; ++q) {
+      const double send = up ? v[q] : v[q + half];
+      const double keep = up ? v[q + half] : v[q];
+      v[q] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  double t = v[0];
+#pragma unroll
+  for (int off = 16 >> p; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+  return t;
+}
+
+// One pass over the rows for basis vectors i0 .. i0 + C - 1 (C independent
+// loads per row), leaving each warp's sums in sm[warp][i0 + c].
+template <int C>
+__device__ __forceinline__ void mdot_pass(int64_t n, const double* __restrict__ V,
+                                          const double* __restrict__ w, int i0,
+                                          double (*sm)[kGMaxK]) {
+  double acc[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) acc[q] = 0.0;
+  const double* Vi = V + (size_t)i0 * n;
+  for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT) {
+    const double wr = w[r];
+    double t[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) t[q] = Vi[(size_t)q * n + r];
+#pragma unroll
+    for (int q = 0; q < C; ++q) acc[q] = fma(t[q], wr, acc[q]);
+  }
+  const double total = scatter_sum<C>(acc);
+  constexpr int low = Scatter<C>::low;
+  const int lane = threadIdx.x & 31, c = lane >> low;
+  if ((lane & ((1 << low) - 1)) == 0 && c < C) sm[threadIdx.x >> 5][i0 + c] = total;
+}
+
+// The last rem (< 16) basis vectors with a pass of exactly that width.
+template <int C>
+__device__ __forceinline__ void mdot_rest(int rem, int64_t n, const double* V, const double* w,
+                                          int i0, double (*sm)[kGMaxK]) {
+  if constexpr (C > 0) {
+    if (rem == C) mdot_pass<C>(n, V, w, i0, sm);
+    else mdot_rest<C - 1>(rem, n, V, w, i0, sm);
+  }
+}
+
 // coef[i] = V_i . w for i <= j (this pass); hcol accumulates the passes.
-__global__ void __launch_bounds__(kGT)
+// Warp sums (scatter_sum) -> CTA sums -> cluster sums in the cluster's
+// first CTA, read through distributed shared memory -> per-cluster partials
+// -> the last cluster to finish adds them, one coefficient per lane.
+__global__ void __cluster_dims__(kGCluster, 1, 1) __launch_bounds__(kGT)
 gm_mdot_kernel(int64_t n, const double* V, const double* w, GmresState* s, GmresWork wk,
                int accumulate, double* partials, unsigned int* counter) {
   pdl_wait();
   pdl_launch_dependents();
+  // Uniform over the grid (nothing writes it during this kernel), so a whole
+  // cluster returns together and no CTA is left at a cluster barrier.
   if (*(volatile int*)&s->not_done == 0) return;
   __shared__ double sm[kGT / 32][kGMaxK];
+  __shared__ double cta[kGMaxK];
   const int k = s->j + 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = 0; i < k; ++i) {
-    const double* Vi = V + (size_t)i * n;
-    double acc = 0.0;
-    for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT)
-      acc = fma(Vi[r], w[r], acc);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) sm[warp][i] = acc;
-  }
+  int i0 = 0;
+  for (; i0 + kGChunk <= k; i0 += kGChunk) mdot_pass<kGChunk>(n, V, w, i0, sm);
+  mdot_rest<kGChunk - 1>(k - i0, n, V, w, i0, sm);
   __syncthreads();
   if (threadIdx.x < k) {
     double t = 0.0;
+#pragma unroll
     for (int q = 0; q < kGT / 32; ++q) t += sm[q][threadIdx.x];
-    partials[(size_t)blockIdx.x * kGMaxK + threadIdx.x] = t;
+    cta[threadIdx.x] = t;
   }
-  if (arrive_last(counter)) {
-    for (int i = warp; i < k; i += kGT / 32) {  // warp w: coefficients w, w+8, ...
-      const double t = warp_total(partials + i, gridDim.x, kGMaxK);
-      if (lane == 0) {
-        wk.coef[i] = t;
-        wk.hcol[i] = accumulate ? wk.hcol[i] + t : t;
+  cg::cluster_group cluster = cg::this_cluster();
+  cluster.sync();
+  const bool leader = cluster.block_rank() == 0;
+  if (leader && threadIdx.x < k) {
+    double v[kGCluster];
+#pragma unroll
+    for (int q = 0; q < kGCluster; ++q) v[q] = cluster.map_shared_rank(cta, q)[threadIdx.x];
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < kGCluster; ++q) t += v[q];
+    partials[(size_t)(blockIdx.x / kGCluster) * kGMaxK + threadIdx.x] = t;
+  }
+  cluster.sync();  // the leader's remote reads are done before any CTA exits
+  if (!leader) return;
+  const unsigned nc = gridDim.x / kGCluster;
+  if (arrive_last(counter, nc)) {
+    // Warp w adds clusters w, w + 8, ... for coefficients lane, lane + 32, ...
+    constexpr int L = (kMdotClusters + kGT / 32 - 1) / (kGT / 32);
+    for (int i = lane; i < k; i += 32) {
+      double v[L];
+#pragma unroll
+      for (int q = 0; q < L; ++q) {
+        const unsigned c = warp + q * (kGT / 32);
+        v[q] = c < nc ? __ldcg(partials + (size_t)c * kGMaxK + i) : 0.0;
       }
+      double t = 0.0;
+#pragma unroll
+      for (int q = 0; q < L; ++q) t += v[q];
+      sm[warp][i] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < k) {
+      double t = 0.0;
+#pragma unroll
+      for (int q = 0; q < kGT / 32; ++q) t += sm[q][threadIdx.x];
+      wk.coef[threadIdx.x] = t;
+      wk.hcol[threadIdx.x] = accumulate ? wk.hcol[threadIdx.x] + t : t;
     }
     if (threadIdx.x == 0) *counter = 0u;
   }
@@ -218,6 +348,29 @@ __device__ void gm_step_finalize(GmresState* s, GmresWork wk, double ww) {
   set_cond(s->while_handle, !stop);
 }
 
+// v - sum_q cf[q] V_{i0+q}[r] for C basis vectors, loads issued together,
+// FMAs in basis order.
+template <int C>
+__device__ __forceinline__ double update_pass(double v, const double* __restrict__ Vi, int64_t n,
+                                              int64_t r, const double* cf) {
+  double t[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) t[q] = Vi[(size_t)q * n + r];
+#pragma unroll
+  for (int q = 0; q < C; ++q) v = fma(-cf[q], t[q], v);
+  return v;
+}
+
+template <int C>
+__device__ __forceinline__ double update_rest(int rem, double v, const double* Vi, int64_t n,
+                                              int64_t r, const double* cf) {
+  if constexpr (C > 0) {
+    if (rem == C) return update_pass<C>(v, Vi, n, r, cf);
+    return update_rest<C - 1>(rem, v, Vi, n, r, cf);
+  }
+  return v;
+}
+
 // w -= sum_i coef[i] V_i; with `norm`, ww = w.w and the step finalize.
 __global__ void __launch_bounds__(kGT)
 gm_update_kernel(int64_t n, const double* V, double* w, GmresState* s, GmresWork wk, int norm,
@@ -233,15 +386,18 @@ gm_update_kernel(int64_t n, const double* V, double* w, GmresState* s, GmresWork
   double acc = 0.0;
   for (int64_t r = (int64_t)blockIdx.x * kGT + threadIdx.x; r < n; r += (int64_t)gridDim.x * kGT) {
     double v = w[r];
-    for (int i = 0; i < k; ++i) v = fma(-cf[i], V[(size_t)i * n + r], v);
+    int i = 0;
+    for (; i + kGChunk <= k; i += kGChunk)
+      v = update_pass<kGChunk>(v, V + (size_t)i * n, n, r, cf + i);
+    v = update_rest<kGChunk - 1>(k - i, v, V + (size_t)i * n, n, r, cf + i);
     w[r] = v;
     acc = fma(v, v, acc);
   }
   if (!norm) return;
   const double c = cta_sum(acc, sm);
   if (threadIdx.x == 0) partials[blockIdx.x] = c;
-  if (arrive_last(counter) && threadIdx.x < 32) {
-    const double t = warp_total(partials, gridDim.x, 1);
+  if (arrive_last(counter, gridDim.x)) {
+    const double t = cta_total(partials, gridDim.x, sm);
     if (threadIdx.x == 0) {
       s->ww = t;
       gm_step_finalize(s, wk, t);
@@ -266,7 +422,7 @@ gm_next_kernel(int64_t n, double* V, const double* w, double* vcur, GmresState* 
     Vn[r] = v;
     vcur[r] = v;
   }
-  if (arrive_last(counter) && threadIdx.x == 0) {
+  if (arrive_last(counter, gridDim.x) && threadIdx.x == 0) {
     s->j = j1;
     *counter = 0u;
   }
@@ -423,7 +579,7 @@ struct Gmres {
     }
     if ((rc = A->apply(in, nullptr, w.p, 1.0, 0.0, guard, nullptr, st))) return rc;
     for (int pass = 0; pass < 2; ++pass) {
-      GBPC_CUDA_TRY(launch_k(gm_mdot_kernel, g_grid(n), kGT, 0, st, n,
+      GBPC_CUDA_TRY(launch_k(gm_mdot_kernel, mdot_grid(n), kGT, 0, st, n,
                              (const double*)V.as<double>(), (const double*)w.as<double>(), S(), W(),
                              pass, partials.as<double>(), counter.as<unsigned int>()));
       GBPC_CUDA_TRY(launch_k(gm_update_kernel, g_grid(n), kGT, 0, st, n,
