@@ -1,0 +1,85 @@
+"""Every sliced-ELL product variant gives the same bits: products, fused dot
+products and whole preconditioned solves, on irregular rows (empty rows,
+lengths 0..40, length-sorted windows) and on the benchmark's operator.
+GBPC_SPMV_VARIANT fixes the variant the autotuner would pick."""
+
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as ss
+import torch
+
+from gpu_helpers import cuda, to_bsr, vec
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = range(5)
+
+
+@pytest.fixture
+def variant_env():
+    old = os.environ.get("GBPC_SPMV_VARIANT")
+    yield
+    if old is None:
+        os.environ.pop("GBPC_SPMV_VARIANT", None)
+    else:
+        os.environ["GBPC_SPMV_VARIANT"] = old
+
+
+def irregular(n, seed):
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 41, size=n)
+    lens[rng.random(n) < 0.05] = 0
+    rows = np.repeat(np.arange(n), lens)
+    cols = rng.integers(0, n, size=rows.size)
+    a = ss.csr_matrix((rng.normal(size=rows.size), (rows, cols)), shape=(n, n))
+    a.sum_duplicates()
+    return a
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_products_identical_across_variants(variant_env, dtype):
+    from warp_preconditioners_gb300 import SparseOperator
+
+    a = irregular(20011, 5)
+    rng = np.random.default_rng(6)
+    x, y = vec(rng.normal(size=a.shape[0]), dtype), vec(rng.normal(size=a.shape[0]), dtype)
+    out = []
+    for v in VARIANTS:
+        os.environ["GBPC_SPMV_VARIANT"] = str(v)
+        A = SparseOperator(to_bsr(a, dtype))
+        z = torch.empty_like(x)
+        A.matvec(x, y, z, 0.7, -0.3)
+        z2 = torch.empty_like(x)
+        A.matvec(x, y, z2, 1.0, 0.0)
+        out.append((z.cpu().numpy(), z2.cpu().numpy()))
+    ref = 0.7 * (a @ x.cpu().double().numpy()) - 0.3 * y.cpu().double().numpy()
+    rtol, atol = (1e-4, 1e-4) if dtype == torch.float32 else (1e-12, 1e-12)
+    np.testing.assert_allclose(out[0][0], ref, rtol=rtol, atol=atol)
+    for v in VARIANTS:
+        np.testing.assert_array_equal(out[v][0], out[0][0])
+        np.testing.assert_array_equal(out[v][1], out[0][1])
+
+
+def test_solves_identical_across_variants(variant_env):
+    # A solve reads every fused dot product's bits: equal iterates after 60
+    # PCG iterations on the factored biharmonic operator mean equal dots.
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, linear, problems
+
+    _, _, K, mass = problems.tet_cube(20)
+    q = problems.biharmonic(K, mass, 1e-4)
+    b = vec(np.random.default_rng(7).normal(size=K.shape[0]))
+    runs = []
+    for v in VARIANTS:
+        os.environ["GBPC_SPMV_VARIANT"] = str(v)
+        free = torch.arange(K.shape[0], dtype=torch.int32, device=cuda())
+        A = SquaredLaplacianOperator(to_bsr(K), vec(mass), free, mass_weight=1e-4)
+        pre = FSAI(to_bsr(q), max_row_size=8)
+        x = torch.zeros_like(b)
+        nit, rr, _ = linear.cg(A, b, x, tol=1e-30, M=pre, maxiter=60, check_every=0)
+        runs.append((int(nit.item()), float(rr.item()), x.cpu().numpy()))
+    assert runs[0][0] == 60
+    for v in VARIANTS:
+        assert runs[v][0] == runs[0][0] and runs[v][1] == runs[0][1]
+        np.testing.assert_array_equal(runs[v][2], runs[0][2])

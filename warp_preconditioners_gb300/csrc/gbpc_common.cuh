@@ -67,7 +67,29 @@ struct SellView {
   const int32_t* cols;
   const V* vals;
   const int32_t* perm;  // stored row k is matrix row perm[k] (nullptr: identity)
+  const int4* sched;    // SliceTask[nslices], slices by width descending
 };
+
+// One entry of a sliced-ELL product schedule: slice s, its width (entries
+// per lane) and the offset of its first entry.  Stored as an int4
+// {s, width, base low word, base high word} so a warp reads it in one load.
+struct SliceTask {
+  int s;
+  int width;
+  int64_t base;
+};
+
+__device__ __forceinline__ SliceTask load_task(const int4* sched, int64_t idx) {
+  const int4 t = __ldg(sched + idx);
+  return SliceTask{t.x, t.y, (int64_t)(((uint64_t)(uint32_t)t.w << 32) | (uint32_t)t.z)};
+}
+
+// Schedule position of a warp's pass i: passes alternate direction over the
+// width-sorted slices (t forward, then W - 1 - t, ...), so a warp that took
+// one of the widest slices of a pass takes one of the narrowest of the next.
+__device__ __forceinline__ int64_t sched_index(int i, int t, int warps_total) {
+  return (int64_t)i * warps_total + ((i & 1) ? warps_total - 1 - t : t);
+}
 
 // ---------------------------------------------------------------------------
 // Krylov scalars, resident on the device for the whole solve.

@@ -76,6 +76,7 @@ struct Sell {
   DevBuf cols;       // int32[nent]
   DevBuf vals;       // vdtype[nent * B * B]
   DevBuf perm;       // int32[nrow] when rows are stored sorted by length
+  DevBuf sched;      // int4[nslices]: product schedule, slices by width descending
   int variant = 0;   // product kernel variant chosen by sell_autotune
   int64_t nnz = 0;   // stored entries without padding
 };

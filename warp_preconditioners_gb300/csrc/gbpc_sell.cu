@@ -15,6 +15,7 @@
 #include <mutex>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "gbpc_common.cuh"
 #include "gbpc_internal.h"
@@ -279,6 +280,41 @@ static void launch_fill(const Sell& s, int B, const int32_t* off, const int32_t*
       s.slice_ptr.as<int64_t>(), s.cols.as<int32_t>(), s.vals.as<VO>());
 }
 
+// Product schedule: the slices by width descending (stable), each entry
+// {slice, width, first entry} as an int4, built on the host from slice_ptr.
+// Rows still sum their entries in storage order; the schedule only decides
+// which warp takes which slice (and so the order of a fused dot product's
+// per-thread partial sums).
+static int build_schedule(Sell& s, cudaStream_t st) {
+  s.sched.release();
+  if (s.nslices == 0) return GBPC_OK;
+  std::vector<int64_t> ptr((size_t)s.nslices + 1);
+  GBPC_CUDA_TRY(cudaMemcpyAsync(ptr.data(), s.slice_ptr.p, sizeof(int64_t) * ptr.size(),
+                                cudaMemcpyDeviceToHost, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int> order((size_t)s.nslices);
+  for (int i = 0; i < s.nslices; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return ptr[a + 1] - ptr[a] > ptr[b + 1] - ptr[b];
+  });
+  std::vector<int32_t> tasks((size_t)4 * s.nslices);
+  for (int i = 0; i < s.nslices; ++i) {
+    const int sl = order[i];
+    const int64_t base = ptr[sl];
+    const uint64_t ubase = (uint64_t)base;
+    tasks[4 * (size_t)i] = sl;
+    tasks[4 * (size_t)i + 1] = (int32_t)((ptr[sl + 1] - base) / kSlice);
+    tasks[4 * (size_t)i + 2] = (int32_t)(uint32_t)(ubase & 0xffffffffu);
+    tasks[4 * (size_t)i + 3] = (int32_t)(uint32_t)(ubase >> 32);
+  }
+  int rc = s.sched.alloc(sizeof(int32_t) * tasks.size());
+  if (rc) return rc;
+  GBPC_CUDA_TRY(cudaMemcpyAsync(s.sched.p, tasks.data(), sizeof(int32_t) * tasks.size(),
+                                cudaMemcpyHostToDevice, st));
+  GBPC_CUDA_TRY(cudaStreamSynchronize(st));
+  return GBPC_OK;
+}
+
 // Rows are sorted by length inside windows when the plain layout would pad
 // more than this fraction.
 constexpr double kSortPadding = 0.10;
@@ -352,6 +388,7 @@ int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const
       s.nent = nent2;
     }
   }
+  if ((rc = build_schedule(s, st))) return rc;
   if ((rc = s.cols.alloc(sizeof(int32_t) * s.nent))) return rc;
   if ((rc = s.vals.alloc(dtype_size(out_dtype) * s.nent * B * B))) return rc;
   if (s.nslices > 0) {
@@ -470,12 +507,29 @@ int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, 
 
 // Kernel variants timed by the autotuner (scalar rows; must match
 // launch_variant in gbpc_spmv.cuh).
-constexpr int kNumVariants = 4;
+constexpr int kNumVariants = 5;
+
+// The software-pipelined variant is the default: inside Krylov iterations
+// (matrix streamed from HBM, input vector warm) it was the fastest or within
+// 2 % on every product of the 70^3 biharmonic solve (forward and backward
+// factored operator, G, G^T).  Another variant replaces it only when it is
+// clearly faster (kSwitchMargin) in the timing below, as can happen on rows
+// much wider than these.
+constexpr int kDefaultVariant = 4;
+constexpr float kSwitchMargin = 0.90f;
 
 int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
   if (m.B != 1 || m.nslices == 0) {
     m.variant = 0;
     return GBPC_OK;
+  }
+  // GBPC_SPMV_VARIANT=0..kNumVariants-1 fixes the variant (tests and
+  // tuning); every variant gives the same results.
+  if (const char* e = std::getenv("GBPC_SPMV_VARIANT")) {
+    if (e[0] >= '0' && e[0] <= '9' && e[1] == '\0' && e[0] - '0' < kNumVariants) {
+      m.variant = e[0] - '0';
+      return GBPC_OK;
+    }
   }
   const size_t vs = dtype_size(adtype);
   DevBuf x, z;
@@ -486,28 +540,24 @@ int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
   cudaEvent_t e0, e1;
   GBPC_CUDA_TRY(cudaEventCreate(&e0));
   GBPC_CUDA_TRY(cudaEventCreate(&e1));
-  float best = 1e30f;
-  int best_v = 0;
-  for (int v = 0; v < kNumVariants; ++v) {
+  float ms[kNumVariants];
+  for (int v = 0; v < kNumVariants && !rc; ++v) {
     m.variant = v;
-    for (int w = 0; w < 2; ++w)
-      if ((rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st)))
-        break;
+    for (int w = 0; w < 2 && !rc; ++w)
+      rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);
     cudaEventRecord(e0, st);
     for (int w = 0; w < 5 && !rc; ++w)
       rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);
     cudaEventRecord(e1, st);
-    if (rc) break;
     cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best) {
-      best = ms;
-      best_v = v;
-    }
+    ms[v] = 0.f;
+    cudaEventElapsedTime(&ms[v], e0, e1);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  int best_v = kDefaultVariant;
+  for (int v = 0; v < kNumVariants && !rc; ++v)
+    if (ms[v] < kSwitchMargin * ms[kDefaultVariant] && ms[v] < ms[best_v]) best_v = v;
   m.variant = best_v;
   if (rc) return rc;
   GBPC_CUDA_TRY(cudaGetLastError());

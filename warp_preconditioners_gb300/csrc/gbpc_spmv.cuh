@@ -104,14 +104,19 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   double dot_part = 0.0;
-  // Warp w of CTA c starts at slice w * gridDim.x + c: the warps of one CTA
-  // work on slices far apart, so rows sorted by length inside windows do not
-  // leave one CTA with all the long rows (its warps wait for each other at
-  // the reduction barrier).
-  for (int s = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; s < m.nslices; s += warps_total) {
-    const int row = s * kSlice + lane;
-    const int64_t base = __ldg(m.slice_ptr + s);
-    const int width = (int)((__ldg(m.slice_ptr + s + 1) - base) >> 5);
+  // Warp w of CTA c is schedule lane t = w * gridDim.x + c (a CTA's warps
+  // sit far apart in the schedule) and takes one slice per pass, passes
+  // alternating direction over the slices sorted by width: every warp gets a
+  // mix of wide and narrow slices, and the slowest warp, which the kernel
+  // waits for, carries close to the average work.
+  const int t = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  for (int i = 0; (int64_t)i * warps_total < m.nslices; ++i) {
+    const int64_t idx = sched_index(i, t, warps_total);
+    if (idx >= m.nslices) break;  // later passes lie further out
+    const SliceTask task = load_task(m.sched, idx);
+    const int row = task.s * kSlice + lane;
+    const int64_t base = task.base;
+    const int width = task.width;
     A acc[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) acc[r] = A(0);
@@ -151,8 +156,8 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
   if (DOT) reduce_and_finalize(red, dot_part);
 }
 
-// Scalar rows, two slices at once: the slices s and s + (warps in the grid)
-// that the loop above would take one after the other are read together, so
+// Scalar rows, two slices at once: the slices of passes i and i + 1 that the
+// loop above would take one after the other are read together, so
 // every lane keeps two independent FMA chains and twice the loads in flight.
 // Each row still sums its entries in storage order, and the dot product
 // receives the rows in the same order, so the result equals the one-slice
@@ -170,16 +175,25 @@ sell_spmv2_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, 
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   double dot_part = 0.0;
-  for (int s = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; s < m.nslices; s += 2 * warps_total) {
-    const int s2 = s + warps_total;
-    const bool has2 = s2 < m.nslices;  // uniform across the warp
-    const int64_t base1 = __ldg(m.slice_ptr + s);
-    const int width1 = (int)((__ldg(m.slice_ptr + s + 1) - base1) >> 5);
+  // Passes i and i + 1 of the one-slice kernel's schedule together.
+  const int t = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  for (int i = 0; (int64_t)i * warps_total < m.nslices; i += 2) {
+    const int64_t idx1 = sched_index(i, t, warps_total);
+    if (idx1 >= m.nslices) break;
+    const int64_t idx2 = sched_index(i + 1, t, warps_total);
+    const bool has2 = idx2 < m.nslices;  // uniform across the warp
+    const SliceTask t1 = load_task(m.sched, idx1);
+    const int s = t1.s;
+    const int64_t base1 = t1.base;
+    const int width1 = t1.width;
+    int s2 = 0;
     int64_t base2 = 0;
     int width2 = 0;
     if (has2) {
-      base2 = __ldg(m.slice_ptr + s2);
-      width2 = (int)((__ldg(m.slice_ptr + s2 + 1) - base2) >> 5);
+      const SliceTask t2 = load_task(m.sched, idx2);
+      s2 = t2.s;
+      base2 = t2.base;
+      width2 = t2.width;
     }
     A acc1[1] = {A(0)}, acc2[1] = {A(0)};
     if (run) {
@@ -220,6 +234,104 @@ sell_spmv2_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, 
   if (DOT) reduce_and_finalize(red, dot_part);
 }
 
+// Chunk ch (CH entries per lane) of a slice into registers: column -1 and
+// value 0 past the slice's width (the same padding the other variants use).
+template <typename V, int CH>
+__device__ __forceinline__ void load_chunk(const SellView<V>& m, const SliceTask& task, int k0,
+                                           int lane, int (&c)[CH], V (&v)[CH]) {
+  const int32_t* cp = m.cols + task.base + lane;
+  const V* vp = m.vals + task.base + lane;
+#pragma unroll
+  for (int j = 0; j < CH; ++j) {
+    const bool in = k0 + j < task.width;
+    c[j] = in ? __ldg(cp + (int64_t)(k0 + j) * kSlice) : -1;
+    v[j] = in ? __ldg(vp + (int64_t)(k0 + j) * kSlice) : static_cast<V>(0.0f);
+  }
+}
+
+// Scalar rows, software-pipelined: a warp walks the chunks of its slices
+// (same schedule as above) as one stream and loads chunk c + 1's columns and
+// values, which come from DRAM, before it gathers x for chunk c (mostly L2
+// hits) and issues chunk c's FMAs, so a warp's own FMAs cover part of its
+// DRAM latency and a slice costs one dependent round trip instead of three.
+// The FMAs, their order and the padding treatment are those of the
+// one-slice kernel, so the results are identical bit for bit.
+template <typename V, typename A, int EPI, bool DOT, int CH>
+__global__ void __launch_bounds__(kThreads, 1)
+sell_spmv_pipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
+                      const int* guard, EpiDev<A> ep, Reduction red) {
+  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  const int t = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  // The matrix does not change while a solve runs (it is written only by
+  // builds and refills, which complete before any product that follows them
+  // starts), so the warp's first schedule entries and first chunk are read
+  // before the wait on the previous kernel: under programmatic dependent
+  // launch these loads overlap that kernel's tail.  Only x, y and the guard
+  // come from the previous kernel.
+  const int64_t idx = sched_index(0, t, warps_total);
+  const bool any = idx < m.nslices;
+  SliceTask cur{-1, 0, 0}, nxt{-1, 0, 0};
+  int pc[CH];
+  V pv[CH];
+  bool have = false;  // pc/pv hold the first chunk of cur
+  if (any) {
+    cur = load_task(m.sched, idx);
+    const int64_t nidx = sched_index(1, t, warps_total);
+    if (nidx < m.nslices) nxt = load_task(m.sched, nidx);
+    if (run) {
+      load_chunk<V, CH>(m, cur, 0, lane, pc, pv);
+      have = true;
+    }
+  }
+  pdl_wait();
+  pdl_launch_dependents();
+  if (guard_off(guard)) return;
+  double dot_part = 0.0;
+  if (any) {
+    int i = 0;
+    while (true) {
+      A acc[1] = {A(0)};
+      if (run) {
+        if (!have) load_chunk<V, CH>(m, cur, 0, lane, pc, pv);
+        have = false;
+        for (int k0 = 0; k0 < cur.width; k0 += CH) {  // uniform across the warp
+          int c[CH];
+          V v[CH];
+#pragma unroll
+          for (int j = 0; j < CH; ++j) {
+            c[j] = pc[j];
+            v[j] = pv[j];
+          }
+          if (k0 + CH < cur.width) {
+            load_chunk<V, CH>(m, cur, k0 + CH, lane, pc, pv);
+          } else if (nxt.s >= 0) {
+            load_chunk<V, CH>(m, nxt, 0, lane, pc, pv);
+            have = true;
+          }
+          A xv[CH];
+#pragma unroll
+          for (int j = 0; j < CH; ++j) xv[j] = (c[j] >= 0) ? __ldg(x + c[j]) : A(0);
+#pragma unroll
+          for (int j = 0; j < CH; ++j)
+            if (k0 + j < cur.width) acc[0] = fma_t<A>(widen<A, V>(v[j]), xv[j], acc[0]);
+        }
+      }
+      spmv_finish<1, V, A, EPI, DOT>(m, cur.s * kSlice + lane, acc, y, z, alpha, beta, run,
+                                     alpha_one, beta_zero, ep, red, dot_part);
+      if (nxt.s < 0) break;
+      cur = nxt;
+      ++i;
+      const int64_t nidx = sched_index(i + 1, t, warps_total);
+      nxt = nidx < m.nslices ? load_task(m.sched, nidx) : SliceTask{-1, 0, 0};
+    }
+  }
+  if (DOT) reduce_and_finalize(red, dot_part);
+}
+
 // Launch configuration of a variant: CTAs resident per SM times SMs, with
 // slices spread over the warps by a grid stride.
 // Every variant launches the same grid (one 1024-thread CTA per SM at most),
@@ -243,9 +355,10 @@ static int spmv_flags(double alpha, double beta) {
 }
 
 // Product kernel variants for scalar rows: entries loaded per chunk 8, 16,
-// 4, and 3 on each of two slices at once; all have a 64-register budget
-// (one 1024-thread CTA per SM).  Blocked rows use one variant.
-constexpr int kNumVariants = 4;
+// 4, 3 on each of two slices at once, and 4 software-pipelined; all have a
+// 64-register budget (one 1024-thread CTA per SM).  Blocked rows use one
+// variant.
+constexpr int kNumVariants = 5;
 
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
 static void launch_one(const SellView<V>& view, const void* x, const void* y, void* z,
@@ -274,6 +387,10 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
         launch_k(sell_spmv2_kernel<V, A, EPI, DOT, 3>, spmv_grid(nslices, 1), kThreads, 0, st,
                  view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
         return;
+      case 4:
+        launch_k(sell_spmv_pipe_kernel<V, A, EPI, DOT, 4>, spmv_grid(nslices, 1), kThreads, 0, st,
+                 view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+        return;
       default:
         break;
     }
@@ -287,7 +404,8 @@ static void launch_spmv(const Sell& m, const void* x, const void* y, void* z, do
                         double beta, const int* guard, const EpiHost& ep, const Reduction& red,
                         cudaStream_t st) {
   SellView<V> view{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
-                   m.vals.as<V>(), m.perm.p ? m.perm.as<int32_t>() : nullptr};
+                   m.vals.as<V>(), m.perm.p ? m.perm.as<int32_t>() : nullptr,
+                   m.sched.as<int4>()};
   EpiDev<A> e{(const A*)ep.aux0, (const A*)ep.aux1};
   const int flags = spmv_flags(alpha, beta);
   if (red.w != nullptr)
