@@ -39,14 +39,22 @@ __device__ __forceinline__ bool inactive(const KrylovScalars* ks) {
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const double* p,
                  const double* Ap, Reduction red) {
+  // x and p are not written by the previous kernel (the operator apply that
+  // produced Ap), so a thread's first row of them is read before the wait.
+  const int64_t i0 = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  double x0 = 0.0, p0 = 0.0;
+  if (i0 < n) {
+    x0 = x[i0];
+    p0 = p[i0];
+  }
   pdl_wait();
   pdl_launch_dependents();
   if (inactive(ks)) return;
   const double alpha = ks->alpha;
   double part = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * kThreads) {
-    x[i] = fma(alpha, p[i], x[i]);
+  for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * kThreads) {
+    const bool first = i == i0;
+    x[i] = fma(alpha, first ? p0 : p[i], first ? x0 : x[i]);
     const double ri = fma(-alpha, Ap[i], r[i]);
     r[i] = ri;
     part = fma(ri, ri, part);
@@ -78,14 +86,22 @@ cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, 
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, const double* w,
             double* q) {
+  // p (and q) were last written an iteration ago, not by the previous
+  // kernel: a thread's first row of them is read before the wait.
+  const int64_t i0 = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  double p0 = 0.0, q0 = 0.0;
+  if (i0 < n) {
+    p0 = p[i0];
+    if (q) q0 = q[i0];
+  }
   pdl_wait();
   pdl_launch_dependents();
   if (inactive(ks)) return;
   const double beta = ks->beta;
-  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * kThreads) {
-    p[i] = fma(beta, p[i], z[i]);
-    if (q) q[i] = fma(beta, q[i], w[i]);
+  for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * kThreads) {
+    const bool first = i == i0;
+    p[i] = fma(beta, first ? p0 : p[i], z[i]);
+    if (q) q[i] = fma(beta, first ? q0 : q[i], w[i]);
   }
 }
 
