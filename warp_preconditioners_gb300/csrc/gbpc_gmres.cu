@@ -301,19 +301,44 @@ gm_mdot_kernel(int64_t n, const double* V, const double* w, GmresState* s, Gmres
   }
 }
 
-// Givens update of column j and the stopping test (one thread).
+// Givens update of column j and the stopping test, by one full warp.
+// Applying rotations 0..j-1 to the new column is the affine recurrence
+// a_{i+1} = -s_i a_i + c_i h_{i+1} (a_0 = h_0) with H[i] = c_i a_i + s_i h_{i+1};
+// the lanes compose the maps with a shuffle scan (5 levels per 32 rotations)
+// instead of one thread stepping through them.
 __device__ void gm_step_finalize(GmresState* s, GmresWork wk, double ww) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   const int j = s->j, m = s->m;
   double* H = wk.H + (size_t)j * (m + 1);
-  for (int i = 0; i <= j; ++i) H[i] = wk.hcol[i];
-  const double hn = sqrt(ww);
-  H[j + 1] = hn;
-  for (int i = 0; i < j; ++i) {
-    const double a = H[i], b = H[i + 1];
-    H[i] = wk.cs[i] * a + wk.sn[i] * b;
-    H[i + 1] = -wk.sn[i] * a + wk.cs[i] * b;
+  double carry = wk.hcol[0];  // a_i at the start of the current block of 32
+  for (int b0 = 0; b0 < j; b0 += 32) {
+    const int i = b0 + lane;
+    const bool on = i < j;
+    const double c = on ? wk.cs[i] : 1.0;
+    const double sn = on ? wk.sn[i] : 0.0;
+    const double h1 = on ? wk.hcol[i + 1] : 0.0;
+    double al = on ? -sn : 1.0, be = on ? c * h1 : 0.0;  // identity past j
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {  // lane i: maps b0..i composed, i's last
+      const double pal = __shfl_up_sync(full, al, o), pbe = __shfl_up_sync(full, be, o);
+      if (lane >= o) {
+        be = fma(al, pbe, be);
+        al = al * pal;
+      }
+    }
+    double pal = __shfl_up_sync(full, al, 1), pbe = __shfl_up_sync(full, be, 1);
+    if (lane == 0) {
+      pal = 1.0;
+      pbe = 0.0;
+    }
+    const double ai = fma(pal, carry, pbe);
+    if (on) H[i] = fma(c, ai, sn * h1);
+    carry = fma(__shfl_sync(full, al, 31), carry, __shfl_sync(full, be, 31));
   }
-  const double a = H[j], b = H[j + 1];
+  if (lane != 0) return;
+  const double hn = sqrt(ww);
+  const double a = carry, b = hn;
   double c = 1.0, sn = 0.0;
   if (b != 0.0) {
     if (fabs(b) > fabs(a)) {
@@ -398,10 +423,13 @@ gm_update_kernel(int64_t n, const double* V, double* w, GmresState* s, GmresWork
   if (threadIdx.x == 0) partials[blockIdx.x] = c;
   if (arrive_last(counter, gridDim.x)) {
     const double t = cta_total(partials, gridDim.x, sm);
-    if (threadIdx.x == 0) {
-      s->ww = t;
-      gm_step_finalize(s, wk, t);
-      *counter = 0u;
+    if (threadIdx.x < 32) {
+      const double ww = __shfl_sync(0xffffffffu, t, 0);
+      if (threadIdx.x == 0) {
+        s->ww = ww;
+        *counter = 0u;
+      }
+      gm_step_finalize(s, wk, ww);
     }
   }
 }
@@ -428,15 +456,35 @@ gm_next_kernel(int64_t n, double* V, const double* w, double* vcur, GmresState* 
   }
 }
 
-// End of a cycle: H y = g by back-substitution (one thread).
+// End of a cycle: H y = g by back-substitution, one warp.  Column-oriented:
+// once y_i is known every lane removes H[r, i] y_i from its rows r < i, so
+// each step is one multiply and one FMA across the lanes; the diagonal
+// reciprocals are formed up front in parallel.
 __global__ void gm_solve_kernel(GmresState* s, GmresWork wk) {
   if (*(volatile int*)&s->restart == 0) return;
-  const int k = s->j + 1, m = s->m;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int k = s->j + 1, m = s->m;  // k <= 64
+  double t0 = 0.0, t1 = 0.0, r0 = 0.0, r1 = 0.0;  // rows lane and lane + 32
+  if (lane < k) {
+    t0 = wk.g[lane];
+    const double d = wk.H[(size_t)lane * (m + 1) + lane];
+    r0 = d != 0.0 ? 1.0 / d : 0.0;
+  }
+  if (lane + 32 < k) {
+    t1 = wk.g[lane + 32];
+    const double d = wk.H[(size_t)(lane + 32) * (m + 1) + lane + 32];
+    r1 = d != 0.0 ? 1.0 / d : 0.0;
+  }
   for (int i = k - 1; i >= 0; --i) {
-    double t = wk.g[i];
-    for (int l = i + 1; l < k; ++l) t -= wk.H[(size_t)l * (m + 1) + i] * wk.y[l];
-    const double d = wk.H[(size_t)i * (m + 1) + i];
-    wk.y[i] = (d != 0.0) ? t / d : 0.0;
+    const bool hi = i >= 32;
+    const double ti = __shfl_sync(full, hi ? t1 : t0, i & 31);
+    const double ri = __shfl_sync(full, hi ? r1 : r0, i & 31);
+    const double yi = ti * ri;
+    if (lane == (i & 31)) wk.y[i] = yi;
+    const double* col = wk.H + (size_t)i * (m + 1);
+    if (lane < i) t0 = fma(-col[lane], yi, t0);
+    if (lane + 32 < i) t1 = fma(-col[lane + 32], yi, t1);
   }
 }
 
@@ -595,7 +643,7 @@ struct Gmres {
   // End of a cycle: y, x += M (V y), and (unless finished) the next residual.
   int record_cycle_end(const double* b, double* x, cudaStream_t st) {
     int rc;
-    gm_solve_kernel<<<1, 1, 0, st>>>(S(), W());
+    gm_solve_kernel<<<1, 32, 0, st>>>(S(), W());
     gm_combine_kernel<<<g_grid(n), kGT, 0, st>>>(n, V.as<double>(), t.as<double>(), S(), W());
     GBPC_CUDA_TRY(cudaGetLastError());
     const double* dx = t.as<double>();
