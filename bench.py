@@ -181,8 +181,10 @@ def cpu_baseline_sample(prob, width, step_size, method, cpu_iters, iterations_pe
     _, it, _, _ = o.krylov(method, A, prob["rhs"][0], M=M, tol=0.0, maxiter=cpu_iters)
     per_iter = (time.perf_counter() - t0) / max(it, 1)
     total = setup + per_iter * sum(iterations_per_rhs)
+    # Operation count of the same setup (untimed: the counting run is separate).
+    flops, _, _ = o.fsai_setup_flops(qc, width=width, step=step_size, tol=1e-3)
     return dict(setup_s=setup, per_iteration_s=per_iter, total_s=total, threads=o.num_threads(),
-                iters_sampled=it)
+                iters_sampled=it, setup_flops=flops)
 
 
 def run_reference(args, prob):
@@ -421,10 +423,26 @@ def main():
                        f"ms each) on one RHS, extrapolated to the GPU's iteration counts "
                        f"{iters[-1]}"),
         }
+        line["fsai_setup_roofline"] = fsai_setup_roofline(cb["setup_flops"],
+                                                          line["refit"]["setup_ms"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+FP64_PEAK_TFLOPS = 1.25  # GB300 nominal FP64; not among the measured peaks
+
+
+def fsai_setup_roofline(flops, setup_ms):
+    """FP64 roofline of the FSAI setup: the oracle's exact operation count of
+    the same setup (each separately rounded multiply, add, divide, square
+    root; the reference evaluates without contraction) over the GPU
+    constructor's CUDA-event time (build, pack, transpose, operator copies)."""
+    achieved = flops / (setup_ms * 1e-3) / 1e12
+    return {"bound": "fp64", "unit": "TFLOP/s", "flops": flops, "setup_ms": setup_ms,
+            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "frac": achieved / FP64_PEAK_TFLOPS,
+            "peak_source": "GB300 nominal FP64 (fallback: no FP64 figure in MEASURED_PEAKS.json)"}
 
 
 def replica_aggregate(elapsed_ms, local_solves, dist, device):

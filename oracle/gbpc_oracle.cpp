@@ -43,6 +43,14 @@ inline T entry(const int32_t* off, const int32_t* col, const T* val, int i, int 
   return result;
 }
 
+// Whether row i stores column j (operation counting only).
+inline bool stored(const int32_t* off, const int32_t* col, int i, int j) {
+  const int32_t* b = col + off[i];
+  const int32_t* e = col + off[i + 1];
+  const int32_t* p = std::lower_bound(b, e, j);
+  return p != e && *p == j;
+}
+
 // warp_preconditioners/fsai.py:44-57 (`diagonal`).
 template <typename T>
 void fsai_diagonal(int n, const int32_t* off, const int32_t* col, const T* val, T* scale,
@@ -64,12 +72,21 @@ void fsai_diagonal(int n, const int32_t* off, const int32_t* col, const T* val, 
 // warp_preconditioners/fsai.py:60-176 (`build`): adaptive support growth with
 // bordered Cholesky, one row at a time.  Returns status increments through
 // `truncated` (status[1]) and `invalid` (status[2]).
-template <typename T>
+//
+// With COUNT, `flops` accumulates the row's floating-point operations: every
+// separately rounded multiply, add/subtract, divide and square root counts
+// one (the reference evaluates without contraction, so there are no fused
+// multiply-adds); comparisons and fabs count none.  A candidate's score term
+// for a support row that does not store the candidate's column is a product
+// with the lookup's zero: it is not counted, since it contributes nothing
+// and a sparse implementation skips it; the small dense Cholesky updates are
+// counted in full.
+template <typename T, bool COUNT = false>
 void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val, const T* scale,
                     T tolerance, T pivot_floor, int width, int step, int32_t* cols_out,
                     T* vals_out, int& truncated, int& invalid, std::vector<int>& pattern,
                     std::vector<T>& chol, std::vector<T>& z, std::vector<T>& v, std::vector<T>& w,
-                    std::vector<int>& cand, std::vector<T>& sc) {
+                    std::vector<int>& cand, std::vector<T>& sc, int64_t& flops) {
   std::fill(pattern.begin(), pattern.end(), -1);
   std::fill(chol.begin(), chol.end(), T(0));
   std::fill(z.begin(), z.end(), T(0));
@@ -96,6 +113,7 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
         T residual = T(0);
         for (int q = 0; q < size; ++q) {
           const int j = pattern[q];
+          if constexpr (COUNT) flops += stored(off, col, c, j) ? 4 : 0;
           // ((a * s_c) * s_j) * z_q, then the running sum: no contraction.
           const T a = entry(off, col, val, c, j);
           const T t1 = a * scale[c];
@@ -125,6 +143,8 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
       if (best < 0 || size == width) break;
       // Border the Cholesky factor of the selected principal submatrix.
       T pivot = T(1);
+      // per p: 2 scalings, p multiply-subtracts, a divide, a square and its subtraction
+      if constexpr (COUNT) flops += 5 * (int64_t)size + (int64_t)size * (size - 1);
       for (int p = 0; p < size; ++p) {
         const T e0 = entry(off, col, val, best, pattern[p]);
         T a = (e0 * scale[best]) * scale[pattern[p]];
@@ -143,6 +163,7 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
       }
       pattern[size] = best;
       for (int p = 0; p < size; ++p) L(size, p) = w[p];
+      if constexpr (COUNT) flops += 1 + 2 * (int64_t)size + 1;  // sqrt, rhs, divide
       L(size, size) = std::sqrt(pivot);
       T rhs = T(0);
       for (int p = 0; p < size; ++p) {
@@ -153,6 +174,7 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
       size += 1;
     }
     // A[S,S] z = e_0 through L^T z = v.
+    if constexpr (COUNT) flops += (int64_t)size + (int64_t)size * (size - 1);
     for (int rev = 0; rev < size; ++rev) {
       const int p = size - 1 - rev;
       T a = v[p];
@@ -164,11 +186,13 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
     }
     if (stopped) break;
     if (tolerance > T(0)) {
+      if constexpr (COUNT) flops += 2;
       const T ratio = old_z0 / z[0];
       if (T(1) - ratio <= tolerance) break;
     }
   }
   const T norm = std::sqrt(z[0]);
+  if constexpr (COUNT) flops += 1 + 2 * (int64_t)size;
   bool valid = true;
   for (int p = 0; p < width; ++p) {
     const size_t e = (size_t)i * width + p;
@@ -184,23 +208,26 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
   if (!valid) invalid += 1;
 }
 
-template <typename T>
+template <typename T, bool COUNT = false>
 void fsai_setup(int n, const int32_t* off, const int32_t* col, const T* val, int width, int step,
                 T tolerance, T pivot_floor, int32_t* cols_out, T* vals_out, T* scale,
-                int32_t* status) {
+                int32_t* status, int64_t* flops_out = nullptr) {
   fsai_diagonal(n, off, col, val, scale, status);
   int truncated = 0, invalid = 0;
-#pragma omp parallel reduction(+ : truncated, invalid)
+  int64_t flops = COUNT ? 2 * (int64_t)n : 0;  // 1 / sqrt(a_ii) per row
+#pragma omp parallel reduction(+ : truncated, invalid, flops)
   {
     std::vector<int> pattern(width), cand(step);
     std::vector<T> chol((size_t)width * width), z(width), v(width), w(width), sc(step);
 #pragma omp for schedule(dynamic, 256)
     for (int i = 0; i < n; ++i)
-      fsai_build_row(i, off, col, val, scale, tolerance, pivot_floor, width, step, cols_out,
-                     vals_out, truncated, invalid, pattern, chol, z, v, w, cand, sc);
+      fsai_build_row<T, COUNT>(i, off, col, val, scale, tolerance, pivot_floor, width, step,
+                               cols_out, vals_out, truncated, invalid, pattern, chol, z, v, w,
+                               cand, sc, flops);
   }
   status[1] += truncated;
   status[2] += invalid;
+  if (flops_out) *flops_out = flops;
 }
 
 // warp_preconditioners/fsai_pack.py:15-71 (`sort_rows`, `array_scan`, `pack`).
@@ -1060,6 +1087,15 @@ void or_fsai_setup_f64(int n, const int32_t* off, const int32_t* col, const doub
                        int width, int step, double tol, double floor_, int32_t* cols_out,
                        double* vals_out, double* scale, int32_t* status) {
   fsai_setup<double>(n, off, col, val, width, step, tol, floor_, cols_out, vals_out, scale, status);
+}
+// FSAI setup that also counts its floating-point operations.
+int64_t or_fsai_setup_flops_f64(int n, const int32_t* off, const int32_t* col, const double* val,
+                                int width, int step, double tol, double floor_, int32_t* cols_out,
+                                double* vals_out, double* scale, int32_t* status) {
+  int64_t flops = 0;
+  fsai_setup<double, true>(n, off, col, val, width, step, tol, floor_, cols_out, vals_out, scale,
+                           status, &flops);
+  return flops;
 }
 void or_fsai_setup_f32(int n, const int32_t* off, const int32_t* col, const float* val, int width,
                        int step, float tol, float floor_, int32_t* cols_out, float* vals_out,

@@ -122,6 +122,27 @@ def fsai_setup(a: CSR, width=8, step=1, tol=1e-3, pivot_floor=None):
     return cols, vals, scale, status
 
 
+def fsai_setup_flops(a: CSR, width=8, step=1, tol=1e-3, pivot_floor=None):
+    """Floating-point operations of the float64 FSAI setup (fsai.py:44-176),
+    counted while the oracle runs it: each separately rounded multiply,
+    add/subtract, divide and square root is one (the reference evaluates
+    without contraction).  Returns (flops, ell_cols, ell_vals)."""
+    a = CSR(a.offsets, a.columns, np.ascontiguousarray(a.values, np.float64), a.ncol)
+    if pivot_floor is None:
+        pivot_floor = 1e-12
+    n = a.nrow
+    cols = np.empty(n * width, np.int32)
+    vals = np.empty(n * width, np.float64)
+    scale = np.empty(n, np.float64)
+    status = np.zeros(3, np.int32)
+    fn = lib().or_fsai_setup_flops_f64
+    fn.restype = ctypes.c_int64
+    flops = fn(n, _p(a.offsets), _p(a.columns), _p(a.values), width, step,
+               ctypes.c_double(tol), ctypes.c_double(pivot_floor), _p(cols), _p(vals), _p(scale),
+               _p(status))
+    return int(flops), cols, vals
+
+
 def fsai_pack(n, width, ell_cols, ell_vals):
     """fsai_pack.py:15-71 — sorts the ELL rows in place, returns CSR G."""
     ell_cols = np.ascontiguousarray(ell_cols, np.int32).copy()

@@ -226,3 +226,28 @@ def test_block_fsai_principal_inverse(oracle):
             np.testing.assert_allclose(row[:, support], expected, rtol=2e-11, atol=1e-10)
         if blocks == 4:
             np.testing.assert_allclose(g.T @ g, np.linalg.inv(a), rtol=2e-11, atol=1e-10)
+
+
+def test_fsai_setup_flop_count():
+    # The counted setup is the same computation: identical factor, and the
+    # count follows the operation tally of fsai.py:44-176 (width 1: one
+    # reciprocal square root per row for the scale, then sqrt(z0) and
+    # (z / norm) * s for the single entry = 5 operations per row).
+    import scipy.sparse as ss
+
+    from oracle import oracle
+
+    a = ss.random(300, 300, density=0.03, random_state=np.random.default_rng(2), format="csr")
+    a = (a + a.T + ss.eye(300) * 8).tocsr()
+    a.sort_indices()
+    c = oracle.CSR.from_scipy(a)
+    f1, _, _ = oracle.fsai_setup_flops(c, width=1)
+    assert f1 == 5 * 300
+    counts = []
+    for width in [2, 4, 8]:
+        flops, cols, vals = oracle.fsai_setup_flops(c, width=width, step=1, tol=0.0)
+        ref_cols, ref_vals, _, _ = oracle.fsai_setup(c, width=width, step=1, tol=0.0)
+        np.testing.assert_array_equal(cols, ref_cols)
+        np.testing.assert_array_equal(vals, ref_vals)
+        counts.append(flops)
+    assert counts[0] < counts[1] < counts[2]

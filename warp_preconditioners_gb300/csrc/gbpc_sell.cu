@@ -153,16 +153,30 @@ __global__ void sell_length_kernel(int nrow, const int32_t* __restrict__ off,
 // Rows ordered by decreasing length inside windows of `window` rows (a stable
 // counting sort per window, one thread per window), so that each 32-row slice
 // holds rows of similar length and padding stays small.
-__global__ void window_sort_kernel(int nrow, int window, int maxlen, const int32_t* __restrict__ len,
-                                   int32_t* perm) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lo = w * window;
-  if (lo >= nrow) return;
-  const int hi = min(nrow, lo + window);
-  int pos = lo;
-  for (int l = maxlen; l >= 0; --l)
-    for (int r = lo; r < hi; ++r)
-      if (len[r] == l) perm[pos++] = r;
+// Rows are sorted by length inside windows when the plain layout would pad
+// more than this fraction.
+constexpr double kSortPadding = 0.10;
+constexpr int kSortWindow = 256;
+
+// Stable sort of each window's rows by length, longest first: one CTA per
+// window, the thread of row r places it at its rank (rows longer than r, or
+// as long and earlier).
+__global__ void __launch_bounds__(kSortWindow)
+window_sort_kernel(int nrow, const int32_t* __restrict__ len, int32_t* perm) {
+  __shared__ int sl[kSortWindow];
+  const int lo = blockIdx.x * kSortWindow;
+  const int hi = min(nrow, lo + kSortWindow);
+  const int k = threadIdx.x;
+  sl[k] = lo + k < hi ? len[lo + k] : -1;
+  __syncthreads();
+  if (lo + k >= hi) return;
+  const int mine = sl[k];
+  int rank = 0;
+  for (int q = 0; q < hi - lo; ++q) {
+    const int o = sl[q];
+    rank += (o > mine) || (o == mine && q < k);
+  }
+  perm[lo + rank] = lo + k;
 }
 
 __global__ void sell_width_kernel(int nrow, int nslices, const int32_t* __restrict__ len,
@@ -315,11 +329,6 @@ static int build_schedule(Sell& s, cudaStream_t st) {
   return GBPC_OK;
 }
 
-// Rows are sorted by length inside windows when the plain layout would pad
-// more than this fraction.
-constexpr double kSortPadding = 0.10;
-constexpr int kSortWindow = 256;
-
 int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const int32_t* col,
                const void* val, int in_dtype, int out_dtype, const SellBuild& opt,
                cudaStream_t st) {
@@ -370,8 +379,8 @@ int sell_build(Sell& s, int nrow_out, int ncol, int B, const int32_t* off, const
     if ((rc = counts2.alloc(sizeof(int64_t) * (s.nslices + 1)))) return rc;
     if ((rc = ptr2.alloc(sizeof(int64_t) * (s.nslices + 1)))) return rc;
     const int nwin = (nrow_out + kSortWindow - 1) / kSortWindow;
-    window_sort_kernel<<<grid_for(nwin, 128), 128, 0, st>>>(nrow_out, kSortWindow, maxlen,
-                                                           len.as<int32_t>(), perm.as<int32_t>());
+    window_sort_kernel<<<nwin, kSortWindow, 0, st>>>(nrow_out, len.as<int32_t>(),
+                                                    perm.as<int32_t>());
     sell_width_kernel<<<grid_for(s.nslices, kThreads), kThreads, 0, st>>>(
         nrow_out, s.nslices, len.as<int32_t>(), perm.as<int32_t>(), counts2.as<int64_t>());
     scan_i64_kernel<<<1, 1024, 0, st>>>(counts2.as<int64_t>(), ptr2.as<int64_t>(), s.nslices);
