@@ -397,6 +397,8 @@ def main():
             "algorithmic_bytes_per_iteration": it_bytes,
             "traffic": traffic,
         },
+        "roofline_fp64": pcg_fp64_roofline(n, prob["K"].nnz, nnz_g, nnz_gt, total_iters,
+                                           solve_total_s),
         "apply_gbps": apply,
         "gpu_launches": launch_count(iters),
     }
@@ -432,6 +434,17 @@ def main():
 
 
 FP64_PEAK_TFLOPS = 1.25  # GB300 nominal FP64; not among the measured peaks
+
+
+def pcg_fp64_roofline(n, nnz_k, nnz_g, nnz_gt, total_iters, solve_s):
+    """The same timed iterations against FP64 arithmetic (a multiply-add is 2
+    flops): 2 per stored entry of the two K products, of G and of G^T, and
+    15 n for the epilogues, the x/r/p updates and the three dot products."""
+    flops = 2 * (2 * nnz_k + nnz_g + nnz_gt) + 15 * n
+    achieved = flops * total_iters / solve_s / 1e12
+    return {"bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops_per_iteration": flops,
+            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "frac": achieved / FP64_PEAK_TFLOPS,
+            "peak_source": "GB300 nominal FP64 (fallback: no FP64 figure in MEASURED_PEAKS.json)"}
 
 
 def fsai_setup_roofline(flops, setup_ms):
