@@ -228,7 +228,12 @@ __device__ __forceinline__ void finalize(const Reduction& red, double total) {
 }
 
 // Every thread of the CTA calls this with its partial; the last CTA to arrive
-// sums all CTA partials in index order and applies the finalize action.
+// sums all CTA partials and applies the finalize action.  That final sum is
+// one warp's: lane l adds partials l, l + 32, ... (loads issued kFinLoads at
+// a time), then a fixed butterfly — fewer barriers and dependent FP64 adds
+// on the critical path than a whole-CTA sum, and the same order every run.
+constexpr int kFinLoads = 10;  // 320 partials per pass: every grid of kSms * kCtasPerSm CTAs
+
 __device__ __forceinline__ void reduce_and_finalize(const Reduction& red, double v) {
   __shared__ double smem[kThreads];
   __shared__ bool am_last;
@@ -240,14 +245,25 @@ __device__ __forceinline__ void reduce_and_finalize(const Reduction& red, double
     am_last = (t == gridDim.x - 1);
   }
   __syncthreads();
-  if (am_last) {
+  if (am_last && threadIdx.x < 32) {
     __threadfence();
+    const unsigned lane = threadIdx.x, count = gridDim.x;
     double acc = 0.0;
-    for (unsigned int k = threadIdx.x; k < gridDim.x; k += kThreads) acc += __ldcg(red.partials + k);
-    const double total = block_sum(acc, smem);
-    if (threadIdx.x == 0) {
+    for (unsigned b = 0; b < count; b += 32 * kFinLoads) {
+      double p[kFinLoads];
+#pragma unroll
+      for (int q = 0; q < kFinLoads; ++q) {
+        const unsigned k = b + lane + 32 * q;
+        p[q] = k < count ? __ldcg(red.partials + k) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < kFinLoads; ++q) acc += p[q];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
       *red.counter = 0u;
-      finalize(red, total);
+      finalize(red, acc);
     }
   }
 }
