@@ -170,16 +170,19 @@ __device__ __forceinline__ void b_reduce(const BRed& red, double v) {
     __threadfence();
     double s = 0.0;
     unsigned int c = warp;
-    // Eight CTA partials loaded together, added in the same order as one at
-    // a time (the sum is unchanged; the loads no longer wait on each other).
-    for (; c + 7 * kBWarps < gridDim.x; c += 8 * kBWarps) {
+    // Eight CTA partials loaded together (zero past the last CTA), added in
+    // the same order as one at a time: the loads no longer wait on each
+    // other, including the last, partial group.
+    for (; c < gridDim.x; c += 8 * kBWarps) {
       double v[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) v[q] = __ldcg(red.partials + (size_t)(c + q * kBWarps) * kB + lane);
+      for (int q = 0; q < 8; ++q) {
+        const unsigned int k = c + q * kBWarps;
+        v[q] = k < gridDim.x ? __ldcg(red.partials + (size_t)k * kB + lane) : 0.0;
+      }
 #pragma unroll
       for (int q = 0; q < 8; ++q) s += v[q];
     }
-    for (; c < gridDim.x; c += kBWarps) s += __ldcg(red.partials + (size_t)c * kB + lane);
     sm[warp][lane] = s;
     __syncthreads();
     if (warp == 0) {
