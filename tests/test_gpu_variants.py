@@ -83,3 +83,36 @@ def test_solves_identical_across_variants(variant_env):
     for v in VARIANTS:
         assert runs[v][0] == runs[0][0] and runs[v][1] == runs[0][1]
         np.testing.assert_array_equal(runs[v][2], runs[0][2])
+
+
+@pytest.mark.parametrize("shape", ["one_row", "n31", "n32", "n33", "empty_rows", "wide"])
+def test_edge_shapes_across_variants(variant_env, shape):
+    from warp_preconditioners_gb300 import SparseOperator
+
+    rng = np.random.default_rng(11)
+    if shape == "one_row":
+        a = ss.csr_matrix(np.array([[2.5]]))
+    elif shape.startswith("n"):
+        n = int(shape[1:])
+        a = ss.random(n, n, density=0.3, random_state=rng, format="csr") + ss.eye(n)
+    elif shape == "empty_rows":
+        a = ss.csr_matrix((300, 300))
+    else:  # rows of 64 entries: many more slices than warps, each several chunks
+        n = 200_000
+        rows = np.repeat(np.arange(n), 64)
+        cols = (rows + rng.integers(0, 4096, size=rows.size)) % n
+        a = ss.csr_matrix((rng.normal(size=rows.size), (rows, cols)), shape=(n, n))
+        a.sum_duplicates()
+    a = ss.csr_matrix(a)
+    x, y = vec(rng.normal(size=a.shape[0])), vec(rng.normal(size=a.shape[0]))
+    ref = 1.5 * (a @ x.cpu().numpy()) + 0.5 * y.cpu().numpy()
+    out = []
+    for v in VARIANTS:
+        os.environ["GBPC_SPMV_VARIANT"] = str(v)
+        A = SparseOperator(to_bsr(a))
+        z = torch.empty_like(x)
+        A.matvec(x, y, z, 1.5, 0.5)
+        out.append(z.cpu().numpy())
+    np.testing.assert_allclose(out[0], ref, rtol=1e-12, atol=1e-12)
+    for v in VARIANTS:
+        np.testing.assert_array_equal(out[v], out[0])
