@@ -62,7 +62,7 @@ def parse_args():
                    help="CG iterations per right-hand side in the CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--config", choices=["c2", "c2sweep", "c3", "c5", "gmres"], default="c2",
+    p.add_argument("--config", choices=["c1", "c2", "c2sweep", "c3", "c5", "gmres"], default="c2",
                    help="c2: biharmonic smoothing (default); c3: K (x) C block coupling, "
                         "every preconditioner under CG and CR; c5: serving stream")
     p.add_argument("--c3-grid", type=int, default=64)
@@ -275,6 +275,10 @@ def main():
     if args.config == "gmres":
         if rank == 0:
             print(json.dumps(run_gmres_steps(args, torch.device("cuda", local))), flush=True)
+        return
+    if args.config == "c1":
+        if rank == 0:
+            print(json.dumps(run_c1(args, torch.device("cuda", local))), flush=True)
         return
     if args.config == "c2sweep":
         if rank == 0:
@@ -754,6 +758,70 @@ def run_gmres_steps(args, dev):
                        "loop": "host" if args.host_loop else "graph"},
             "metric": "ms per Arnoldi step", "steps": steps,
             "ms_per_step": e0.elapsed_time(e1) / max(steps, 1)}
+
+
+def run_c1(args, dev):
+    """The reference's CPU-runnable case: 64 x 64 interior 5-point Dirichlet
+    Laplacian (4,096 unknowns, unscaled stencil), U[-1,1] right-hand side
+    (seed 0), FSAI w8 step 1 kap 1e-3, CG to 1e-8 from x = 0.  GPU setup and
+    solve are CUDA-event medians of 5 (the solve is one graph launch); the
+    oracle (CPU restatement, all host threads) runs the same setup and solve
+    as the CPU baseline, and its iteration count and solution are the
+    parity check."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, from_scipy, linear, problems
+
+    torch.cuda.set_device(dev)
+    a = problems.laplacian_2d(64)
+    b_np = problems.uniform_rhs(a.shape[0], 0)
+    A = from_scipy(a, dev)
+    b = torch.as_tensor(b_np, device=dev)
+    x = torch.zeros_like(b)
+
+    def timed(fn, reps=5):
+        out = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return statistics.median(out), r
+
+    setup_ms, pre = timed(lambda: FSAI(A, max_row_size=8, max_step_size=1, kap_tolerance=1e-3))
+    solver = linear.Solver("cg", A, pre)
+
+    def solve():
+        x.zero_()
+        return solver.run(b, x, tol=args.rtol, maxiter=10000)
+
+    solve()
+    solve_ms, (nit, rr, atol_sq) = timed(solve)
+    out = {"config": {"workload": "C1: 64x64 5-point Dirichlet Laplacian (4,096 unknowns), "
+                                  "FSAI w8 step 1 kap 1e-3, CG to %g, x0 = 0" % args.rtol},
+           "setup_ms": setup_ms, "solve_ms": solve_ms, "iterations": int(nit.item()),
+           "converged": bool(rr.item() <= atol_sq.item()),
+           "true_relres": float(np.linalg.norm(b_np - a @ x.cpu().numpy()) / np.linalg.norm(b_np))}
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+
+        c = oracle.CSR(a.indptr, a.indices, a.data)
+        t0 = time.perf_counter()
+        g, gt, _ = oracle.fsai(c, width=8, step=1, tol=1e-3)
+        t1 = time.perf_counter()
+        x_or, it_or, _, _ = oracle.krylov("cg", oracle.Operator.csr(c), b_np,
+                                          M=oracle.Operator.fsai(g, gt), tol=args.rtol,
+                                          maxiter=10000)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"setup_ms": (t1 - t0) * 1e3, "solve_ms": (t2 - t1) * 1e3,
+                               "iterations": it_or, "cores": oracle.num_threads(),
+                               "kind": "port",
+                               "max_rel_diff_x": float(np.max(np.abs(x.cpu().numpy() - x_or))
+                                                       / np.max(np.abs(x_or)))}
+    return out
 
 
 def run_c2_sweep(args, dev):
