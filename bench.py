@@ -1059,7 +1059,11 @@ def launch_count(iters):
 
 
 def measure_applies(pre, K, mass, free, n, dev):
-    """Live CUDA-event timing of the two applies on the step's data (GB/s)."""
+    """Live CUDA-event timing of the two applies on the step's data: 50
+    back-to-back applies replayed from one graph, algorithmic bytes over the
+    time (GB/s).  The FSAI factor (66 MB) stays in L2 between them, so this
+    is the apply's FP64-bound rate, not an HBM figure (the PCG roofline is
+    the HBM one)."""
     import torch
 
     from warp_preconditioners_gb300 import SquaredLaplacianOperator
