@@ -405,7 +405,7 @@ fsai_build_kernel(BuildParams P, const int32_t* __restrict__ off, const int32_t*
 }
 
 // ---------------------------------------------------------------------------
-// The same build for widths <= 16 with lanes = rows: a warp owns 32
+// The same build for widths <= 48 with lanes = rows: a warp owns 32
 // consecutive rows.  Candidate scoring and selection stay cooperative, one
 // row at a time (every lane on a slice of that row's frontier, as above),
 // but the bordered factorisation, the substitution L^T z = v and the stop
@@ -1104,13 +1104,15 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
   };
-  // First pass: lanes = rows for widths <= 16 (see fsai_build_lanes_kernel).
+  // First pass: lanes = rows for widths <= 48 (see fsai_build_lanes_kernel;
+  // at 48 the per-thread factor, 10.6 KB in float64, lives in local memory).
   auto launch_lanes = [&](int H, int hbits) -> int {
     const int SC = std::min(S, W);
     const size_t per_warp = lanes_smem_bytes((int)sizeof(T), W, SC, H);
     const size_t smem = per_warp * kLanesWarps;
     if (smem > (size_t)smem_optin) return launch(H, hbits, nullptr, n);
-    auto kern = (W <= 8) ? fsai_build_lanes_kernel<T, 8> : fsai_build_lanes_kernel<T, 16>;
+    auto kern = (W <= 8) ? fsai_build_lanes_kernel<T, 8>
+                : (W <= 16) ? fsai_build_lanes_kernel<T, 16> : fsai_build_lanes_kernel<T, 48>;
     GBPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
     BuildParams P;
@@ -1133,7 +1135,7 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
   };
-  if (W <= 16 && lanes_build_enabled()) {
+  if (W <= 48 && lanes_build_enabled()) {
     if ((rc = launch_lanes(Hfirst, hbits_first))) return rc;
   } else if ((rc = launch(Hfirst, hbits_first, nullptr, n))) {
     return rc;
