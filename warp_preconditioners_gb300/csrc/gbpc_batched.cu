@@ -230,12 +230,31 @@ bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __
       int maxlen = len;
 #pragma unroll
       for (int o = KP; o < 32; o <<= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
-      for (int base = 0; base < maxlen; base += KP) {
-        if constexpr (KP == 1) {
-          if (base < len)
-            acc = fma_bt<T>(cvt<T, V>(__ldg(val + e0 + base)),
-                            X[(int64_t)__ldg(col + e0 + base) * k], acc);
-        } else {
+      // Gathers of a chunk are issued together, then the FMAs run in
+      // storage order (the same sum as one entry at a time).  The FMA loops
+      // stop at the chunk's last entry in any row of the warp (a uniform
+      // exit): an FP64 instruction costs its full issue slot even with every
+      // lane predicated off.
+      if constexpr (KP == 1) {
+        constexpr int U = 4;
+        for (int base = 0; base < maxlen; base += U) {
+          T xv[U], vv[U];
+#pragma unroll
+          for (int e = 0; e < U; ++e) {
+            const bool in = base + e < len;
+            vv[e] = in ? cvt<T, V>(__ldg(val + e0 + base + e)) : T(0);
+            xv[e] = in ? X[(int64_t)__ldg(col + e0 + base + e) * k] : T(0);
+          }
+#pragma unroll
+          for (int e = 0; e < U; ++e) {
+            if (base + e >= maxlen) break;
+            if (base + e < len) acc = fma_bt<T>(vv[e], xv[e], acc);
+          }
+        }
+      } else if constexpr (KP >= 16) {
+        // Wide groups: enough independent work per warp already; one
+        // entry at a time (the batched form measured slower and spills).
+        for (int base = 0; base < maxlen; base += KP) {
           int c_l = 0;
           T v_l = T(0);
           if (base + j < len) {
@@ -247,6 +266,33 @@ bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __
             const int c = __shfl_sync(0xffffffffu, c_l, e, KP);
             const T v = __shfl_sync(0xffffffffu, v_l, e, KP);
             if (on && base + e < len) acc = fma_bt<T>(v, X[(int64_t)c * k + j], acc);
+          }
+        }
+      } else {
+        constexpr int SUB = KP;  // all the chunk's gathers in flight per lane
+        for (int base = 0; base < maxlen; base += KP) {
+          int c_l = 0;
+          T v_l = T(0);
+          if (base + j < len) {
+            c_l = __ldg(col + e0 + base + j);
+            v_l = cvt<T, V>(__ldg(val + e0 + base + j));
+          }
+          const int cnt = min(KP, maxlen - base);
+#pragma unroll
+          for (int s0 = 0; s0 < KP; s0 += SUB) {
+            if (s0 >= cnt) break;
+            T xv[SUB], vv[SUB];
+#pragma unroll
+            for (int e = 0; e < SUB; ++e) {
+              const int c = __shfl_sync(0xffffffffu, c_l, s0 + e, KP);
+              vv[e] = __shfl_sync(0xffffffffu, v_l, s0 + e, KP);
+              xv[e] = (on && base + s0 + e < len) ? X[(int64_t)c * k + j] : T(0);
+            }
+#pragma unroll
+            for (int e = 0; e < SUB; ++e) {
+              if (s0 + e >= cnt) break;
+              if (on && base + s0 + e < len) acc = fma_bt<T>(vv[e], xv[e], acc);
+            }
           }
         }
       }
