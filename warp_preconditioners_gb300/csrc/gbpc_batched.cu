@@ -201,12 +201,19 @@ enum BEpi : int { BE_AXPBY = 0, BE_SQLAP_BWD = 1 };
 // handles 32/KP consecutive rows, one per group of KP lanes; lane j of a
 // group works on right-hand side j.  Row-scaled forward products pass the
 // scaled matrix.  Each row sums its entries in storage order, whatever KP.
-template <typename V, typename T, int EPI, bool DOT, int KP>
+// UNIT: alpha == 1 and beta == 0 known at compile time (the Krylov loops'
+// products), so no scaling or Y term is issued.
+template <typename V, typename T, int EPI, bool DOT, int KP, bool UNIT = false>
 __global__ void __launch_bounds__(kBThreads, 2)
 bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __restrict__ col,
              const V* __restrict__ val, const T* X, const T* Y, T* Z, double alpha, double beta,
              int alpha_zero, int alpha_one, int beta_zero, const T* wm, const T* X2,
              const int* guard, BRed red) {
+  if constexpr (UNIT) {
+    alpha_zero = 0;
+    alpha_one = 1;
+    beta_zero = 1;
+  }
   pdl_wait();
   pdl_launch_dependents();
   if (guard_off(guard)) return;
@@ -509,16 +516,20 @@ static void launch_bspmm(const BCsr& m, int k, const void* X, const void* Y, voi
   with_kp(k, [&](auto kpc) {
     constexpr int KP = decltype(kpc)::value;
     const int g = b_grid(m.nrow, KP);
-    if (dot && dot->w)
-      launch_k(bspmm_kernel<V, T, EPI, true, KP>, g, kBThreads, 0, st, m.nrow, k,
-               (const int32_t*)m.off.as<int32_t>(), (const int32_t*)m.col.as<int32_t>(),
-               (const V*)m.val.as<V>(), (const T*)X, (const T*)Y, (T*)Z, alpha, beta, az, a1, bz,
-               (const T*)wm, (const T*)X2, guard, red);
-    else
-      launch_k(bspmm_kernel<V, T, EPI, false, KP>, g, kBThreads, 0, st, m.nrow, k,
-               (const int32_t*)m.off.as<int32_t>(), (const int32_t*)m.col.as<int32_t>(),
-               (const V*)m.val.as<V>(), (const T*)X, (const T*)Y, (T*)Z, alpha, beta, az, a1, bz,
-               (const T*)wm, (const T*)X2, guard, red);
+    auto go = [&](auto kern) {
+      launch_k(kern, g, kBThreads, 0, st, m.nrow, k, (const int32_t*)m.off.as<int32_t>(),
+               (const int32_t*)m.col.as<int32_t>(), (const V*)m.val.as<V>(), (const T*)X,
+               (const T*)Y, (T*)Z, alpha, beta, az, a1, bz, (const T*)wm, (const T*)X2, guard,
+               red);
+    };
+    const bool unit = !az && a1 && bz;
+    if (dot && dot->w) {
+      if (unit) go(bspmm_kernel<V, T, EPI, true, KP, true>);
+      else go(bspmm_kernel<V, T, EPI, true, KP>);
+    } else {
+      if (unit) go(bspmm_kernel<V, T, EPI, false, KP, true>);
+      else go(bspmm_kernel<V, T, EPI, false, KP>);
+    }
   });
 }
 

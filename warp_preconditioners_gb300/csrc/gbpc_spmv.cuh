@@ -256,13 +256,16 @@ __device__ __forceinline__ void load_chunk(const SellView<V>& m, const SliceTask
 // DRAM latency and a slice costs one dependent round trip instead of three.
 // The FMAs, their order and the padding treatment are those of the
 // one-slice kernel, so the results are identical bit for bit.
-template <typename V, typename A, int EPI, bool DOT, int CH>
+// UNIT: alpha == 1 and beta == 0 known at compile time (every product of
+// the Krylov loops), so the epilogue carries no scaling or y term at all.
+template <typename V, typename A, int EPI, bool DOT, int CH, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, 1)
 sell_spmv_pipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
                       const int* guard, EpiDev<A> ep, Reduction red) {
-  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
-  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
-  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
+  const bool run =
+      UNIT || (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = UNIT || (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = UNIT || (flags & F_BETA_ZERO) != 0;
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   const int t = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
@@ -388,8 +391,14 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
                  view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
         return;
       case 4:
-        launch_k(sell_spmv_pipe_kernel<V, A, EPI, DOT, 4>, spmv_grid(nslices, 1), kThreads, 0, st,
-                 view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+        if (flags == (F_ALPHA_ONE | F_BETA_ZERO))
+          launch_k(sell_spmv_pipe_kernel<V, A, EPI, DOT, 4, true>, spmv_grid(nslices, 1), kThreads,
+                   0, st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e,
+                   red);
+        else
+          launch_k(sell_spmv_pipe_kernel<V, A, EPI, DOT, 4>, spmv_grid(nslices, 1), kThreads, 0,
+                   st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e,
+                   red);
         return;
       default:
         break;
