@@ -82,7 +82,9 @@ cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, 
   reduce_and_finalize(red, part);
 }
 
-// p = z + beta p  (and q = w + beta q when q != nullptr)
+// p = z + beta p  (and q = w + beta q with Q: CR).  Q is a template
+// parameter so that CG issues no FP64 instruction for the absent q.
+template <bool Q>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, const double* w,
             double* q) {
@@ -92,7 +94,7 @@ xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, cons
   double p0 = 0.0, q0 = 0.0;
   if (i0 < n) {
     p0 = p[i0];
-    if (q) q0 = q[i0];
+    if (Q) q0 = q[i0];
   }
   pdl_wait();
   pdl_launch_dependents();
@@ -101,7 +103,7 @@ xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, cons
   for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * kThreads) {
     const bool first = i == i0;
     p[i] = fma(beta, first ? p0 : p[i], z[i]);
-    if (q) q[i] = fma(beta, first ? q0 : q[i], w[i]);
+    if (Q) q[i] = fma(beta, first ? q0 : q[i], w[i]);
   }
 }
 
@@ -238,7 +240,7 @@ struct Solver {
                              (const double*)Ap.as<double>(), rrr));
       DotSpec db = dot(r.as<double>(), FIN_CG_BETA);
       if ((rc = precondition(r.as<double>(), z.as<double>(), guard, &db, st))) return rc;
-      GBPC_CUDA_TRY(launch_k(xpay_kernel, vec_grid(n), kThreads, 0, st, n,
+      GBPC_CUDA_TRY(launch_k(xpay_kernel<false>, vec_grid(n), kThreads, 0, st, n,
                              (const KrylovScalars*)K(), (const double*)z.as<double>(),
                              p.as<double>(), (const double*)nullptr, (double*)nullptr));
     } else {
@@ -249,7 +251,7 @@ struct Solver {
                              (const double*)Ap.as<double>(), (const double*)y.as<double>(), rrr));
       DotSpec db = dot(z.as<double>(), FIN_CG_BETA);
       if ((rc = A->apply(z.p, nullptr, Az.p, 1.0, 0.0, guard, &db, st))) return rc;
-      GBPC_CUDA_TRY(launch_k(xpay_kernel, vec_grid(n), kThreads, 0, st, n,
+      GBPC_CUDA_TRY(launch_k(xpay_kernel<true>, vec_grid(n), kThreads, 0, st, n,
                              (const KrylovScalars*)K(), (const double*)z.as<double>(),
                              p.as<double>(), (const double*)Az.as<double>(), Ap.as<double>()));
     }

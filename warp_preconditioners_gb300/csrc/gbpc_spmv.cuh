@@ -90,7 +90,7 @@ __device__ __forceinline__ void spmv_finish(const SellView<V>& m, int row, const
   }
 }
 
-template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
+template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, MINB)
 sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
                  const int* guard, EpiDev<A> ep, Reduction red) {
@@ -98,9 +98,10 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
   pdl_launch_dependents();
   if (guard_off(guard)) return;
   constexpr int BB = B * B;
-  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
-  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
-  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
+  const bool run =
+      UNIT || (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = UNIT || (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = UNIT || (flags & F_BETA_ZERO) != 0;
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   double dot_part = 0.0;
@@ -162,16 +163,17 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
 // Each row still sums its entries in storage order, and the dot product
 // receives the rows in the same order, so the result equals the one-slice
 // kernel's bit for bit.
-template <typename V, typename A, int EPI, bool DOT, int CH>
+template <typename V, typename A, int EPI, bool DOT, int CH, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, 1)
 sell_spmv2_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
                   const int* guard, EpiDev<A> ep, Reduction red) {
   pdl_wait();
   pdl_launch_dependents();
   if (guard_off(guard)) return;
-  const bool run = (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
-  const bool alpha_one = (flags & F_ALPHA_ONE) != 0;
-  const bool beta_zero = (flags & F_BETA_ZERO) != 0;
+  const bool run =
+      UNIT || (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = UNIT || (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = UNIT || (flags & F_BETA_ZERO) != 0;
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (kThreads / 32);
   double dot_part = 0.0;
@@ -363,12 +365,22 @@ static int spmv_flags(double alpha, double beta) {
 // variant.
 constexpr int kNumVariants = 5;
 
+// Products with alpha == 1 and beta == 0 (all of the Krylov loops') run an
+// instantiation that knows it: no scaling or y term is issued (an FP64
+// instruction costs its issue slot even with every lane predicated off).
+constexpr int kUnitFlags = F_ALPHA_ONE | F_BETA_ZERO;
+
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
 static void launch_one(const SellView<V>& view, const void* x, const void* y, void* z,
                        double alpha, double beta, int flags, const int* guard, const EpiDev<A>& e,
                        const Reduction& red, int nslices, cudaStream_t st) {
-  launch_k(sell_spmv_kernel<B, V, A, EPI, DOT, CH, MINB>, spmv_grid(nslices, MINB), kThreads, 0,
-           st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+  if (flags == kUnitFlags)
+    launch_k(sell_spmv_kernel<B, V, A, EPI, DOT, CH, MINB, true>, spmv_grid(nslices, MINB),
+             kThreads, 0, st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags,
+             guard, e, red);
+  else
+    launch_k(sell_spmv_kernel<B, V, A, EPI, DOT, CH, MINB>, spmv_grid(nslices, MINB), kThreads, 0,
+             st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
 }
 
 template <int B, typename V, typename A, int EPI, bool DOT>
@@ -387,11 +399,16 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
                                             nslices, st);
         return;
       case 3:
-        launch_k(sell_spmv2_kernel<V, A, EPI, DOT, 3>, spmv_grid(nslices, 1), kThreads, 0, st,
-                 view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+        if (flags == kUnitFlags)
+          launch_k(sell_spmv2_kernel<V, A, EPI, DOT, 3, true>, spmv_grid(nslices, 1), kThreads, 0,
+                   st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e,
+                   red);
+        else
+          launch_k(sell_spmv2_kernel<V, A, EPI, DOT, 3>, spmv_grid(nslices, 1), kThreads, 0, st,
+                   view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
         return;
       case 4:
-        if (flags == (F_ALPHA_ONE | F_BETA_ZERO))
+        if (flags == kUnitFlags)
           launch_k(sell_spmv_pipe_kernel<V, A, EPI, DOT, 4, true>, spmv_grid(nslices, 1), kThreads,
                    0, st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e,
                    red);
