@@ -28,7 +28,8 @@ namespace {
 // Elementwise kernels.
 
 // z = alpha * (d .* x) + beta * y   (d == nullptr: d = 1), optional dot(w, z).
-template <typename A>
+// UNIT: alpha == 1 and beta == 0 known at compile time (1 * t == t).
+template <typename A, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 scale_axpby_kernel(int64_t n, const A* d, const A* x, const A* y, A* z, A alpha, A beta,
                    const int* guard, Reduction red) {
@@ -37,8 +38,9 @@ scale_axpby_kernel(int64_t n, const A* d, const A* x, const A* y, A* z, A alpha,
   for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kThreads) {
     A v = A(0);
-    if (alpha != A(0)) v = alpha * (d ? d[i] * x[i] : x[i]);
-    if (beta != A(0)) v = v + beta * y[i];
+    if (UNIT) v = d ? d[i] * x[i] : x[i];
+    else if (alpha != A(0)) v = alpha * (d ? d[i] * x[i] : x[i]);
+    if (!UNIT && beta != A(0)) v = v + beta * y[i];
     z[i] = v;
     if (red.w) part = fma((double)v, red.w[i], part);
   }
@@ -46,10 +48,16 @@ scale_axpby_kernel(int64_t n, const A* d, const A* x, const A* y, A* z, A alpha,
 }
 
 // Block diagonal apply: z_i = alpha * inv_i x_i + beta y_i (block_ilu.py:188-202).
-template <typename A, int B>
+// UNIT: alpha == 1 and beta == 0 known at compile time (inside the Krylov
+// loops), so neither the scaling (1 * s == s) nor the y term is issued.
+template <typename A, int B, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 block_diag_apply_kernel(int nrow, const A* __restrict__ inv, const A* x, const A* y, A* z, A alpha,
                         A beta, const int* guard, Reduction red) {
+  if constexpr (UNIT) {
+    alpha = A(1);
+    beta = A(0);
+  }
   if (guard_off(guard)) return;
   double part = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < nrow; i += gridDim.x * kThreads) {
@@ -65,7 +73,7 @@ block_diag_apply_kernel(int nrow, const A* __restrict__ inv, const A* x, const A
         A s = A(0);
 #pragma unroll
         for (int q = 0; q < B; ++q) s = fma(inv[(int64_t)i * B * B + r * B + q], xi[q], s);
-        v[r] = alpha * s;
+        v[r] = UNIT ? s : alpha * s;
       }
     }
 #pragma unroll
@@ -160,7 +168,10 @@ Reduction make_reduction(const DotSpec* dot) {
 int scale_axpby(int vdtype, int64_t n, const void* d, const void* x, const void* y, void* z,
                 double alpha, double beta, const int* guard, const DotSpec* dot, cudaStream_t st) {
   const Reduction red = make_reduction(dot);
-  if (vdtype == GBPC_F64)
+  if (vdtype == GBPC_F64 && alpha == 1.0 && beta == 0.0)
+    scale_axpby_kernel<double, true><<<elementwise_grid(n), kThreads, 0, st>>>(
+        n, (const double*)d, (const double*)x, (const double*)y, (double*)z, alpha, beta, guard, red);
+  else if (vdtype == GBPC_F64)
     scale_axpby_kernel<double><<<elementwise_grid(n), kThreads, 0, st>>>(
         n, (const double*)d, (const double*)x, (const double*)y, (double*)z, alpha, beta, guard, red);
   else
@@ -241,8 +252,13 @@ struct BlockJacobiOp : Operator {
             const DotSpec* dot, cudaStream_t st) override {
     const Reduction red = make_reduction(dot);
     const int g = elementwise_grid(nrow);
+    const bool unit = alpha == 1.0 && beta == 0.0;
 #define GBPC_BJ(Bv)                                                                            \
-  if (vdtype == GBPC_F64)                                                                      \
+  if (vdtype == GBPC_F64 && unit)                                                              \
+    block_diag_apply_kernel<double, Bv, true><<<g, kThreads, 0, st>>>(                         \
+        nrow, inv.as<double>(), (const double*)x, (const double*)y, (double*)z, alpha, beta,    \
+        guard, red);                                                                           \
+  else if (vdtype == GBPC_F64)                                                                 \
     block_diag_apply_kernel<double, Bv><<<g, kThreads, 0, st>>>(                               \
         nrow, inv.as<double>(), (const double*)x, (const double*)y, (double*)z, alpha, beta,    \
         guard, red);                                                                           \
