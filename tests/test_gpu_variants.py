@@ -116,3 +116,25 @@ def test_edge_shapes_across_variants(variant_env, shape):
     np.testing.assert_allclose(out[0], ref, rtol=1e-12, atol=1e-12)
     for v in VARIANTS:
         np.testing.assert_array_equal(out[v], out[0])
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_unit_scaling_products_equal_general_path(variant_env, dtype):
+    # alpha = 1, beta = 0 runs the instantiation that issues no scaling or y
+    # term; alpha = 1, beta = 1 with y = 0 runs the run-time-flag path and
+    # adds exact zeros.  Every variant must give the same bits both ways.
+    from warp_preconditioners_gb300 import FSAI, SparseOperator, problems
+
+    a = irregular(20011, 9)
+    q = problems.laplacian_2d(40)
+    rng = np.random.default_rng(10)
+    for v in VARIANTS:
+        os.environ["GBPC_SPMV_VARIANT"] = str(v)
+        for op, n in ((SparseOperator(to_bsr(a, dtype)), a.shape[0]),
+                      (FSAI(to_bsr(q, dtype), max_row_size=8), q.shape[0])):
+            x = vec(rng.normal(size=n), dtype)
+            zeros = torch.zeros_like(x)
+            z_unit, z_gen = torch.empty_like(x), torch.empty_like(x)
+            op.matvec(x, x, z_unit, 1.0, 0.0)
+            op.matvec(x, zeros, z_gen, 1.0, 1.0)
+            np.testing.assert_array_equal(z_unit.cpu().numpy(), z_gen.cpu().numpy())
