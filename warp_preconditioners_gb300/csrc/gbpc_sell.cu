@@ -540,6 +540,13 @@ int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
       return GBPC_OK;
     }
   }
+  // Fewer slices than warps in one grid (kSms CTAs of kThreads): the
+  // product is launch-latency-bound and timing the variants measures noise,
+  // so the default stands without the 35 timed launches.
+  if (m.nslices < kSms * (kThreads / 32)) {
+    m.variant = kDefaultVariant;
+    return GBPC_OK;
+  }
   const size_t vs = dtype_size(adtype);
   DevBuf x, z;
   int rc;
