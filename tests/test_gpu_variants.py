@@ -138,3 +138,56 @@ def test_unit_scaling_products_equal_general_path(variant_env, dtype):
             op.matvec(x, x, z_unit, 1.0, 0.0)
             op.matvec(x, zeros, z_gen, 1.0, 1.0)
             np.testing.assert_array_equal(z_unit.cpu().numpy(), z_gen.cpu().numpy())
+
+
+@pytest.mark.parametrize("block", [2, 3])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_blocked_products_identical_across_variants(variant_env, block, dtype):
+    # Variant 4 on blocked rows is the pipelined blocked kernel; it must give
+    # the one-slice blocked kernel's bits (rows of 0..14 blocks, empty rows).
+    from warp_preconditioners_gb300 import SparseOperator
+
+    rng = np.random.default_rng(12 + block)
+    nb = 12007
+    lens = rng.integers(0, 15, size=nb)
+    rows = np.repeat(np.arange(nb), lens)
+    cols = rng.integers(0, nb, size=rows.size)
+    blocks = ss.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(nb, nb))
+    blocks.sum_duplicates()
+    dense_pattern = ss.kron(blocks, np.ones((block, block)), format="csr")
+    a = dense_pattern.multiply(rng.normal(size=dense_pattern.shape[0])[:, None]).tocsr()
+    a.data = rng.normal(size=a.nnz)
+    n = a.shape[0]
+    x, y = vec(rng.normal(size=n), dtype), vec(rng.normal(size=n), dtype)
+    out = {}
+    for v in (0, 4):
+        os.environ["GBPC_SPMV_VARIANT"] = str(v)
+        A = SparseOperator(to_bsr(a, dtype, block))
+        z1, z2 = torch.empty_like(x), torch.empty_like(x)
+        A.matvec(x, y, z1, 0.7, -0.3)
+        A.matvec(x, y, z2, 1.0, 0.0)
+        out[v] = (z1.cpu().numpy(), z2.cpu().numpy())
+    ref = 0.7 * (a @ x.cpu().double().numpy()) - 0.3 * y.cpu().double().numpy()
+    rtol, atol = (1e-4, 1e-4) if dtype == torch.float32 else (1e-12, 1e-12)
+    np.testing.assert_allclose(out[0][0], ref, rtol=rtol, atol=atol)
+    for k in range(2):
+        np.testing.assert_array_equal(out[4][k], out[0][k])
+
+
+def test_blocked_solves_identical_across_variants(variant_env):
+    # Fixed-iteration block-Jacobi CG on the K (x) C coupling: equal iterates
+    # mean equal fused dots on 3 x 3 blocks.
+    from warp_preconditioners_gb300 import BlockJacobi, SparseOperator, linear, problems
+
+    bsr, _ = problems.kron_coupling(24, 1e-6)
+    b = vec(np.random.default_rng(13).normal(size=bsr.shape[0]))
+    xs = []
+    for v in (0, 4):
+        os.environ["GBPC_SPMV_VARIANT"] = str(v)
+        A = SparseOperator(to_bsr(bsr, block=3))
+        M = BlockJacobi(to_bsr(bsr, block=3))
+        x = torch.zeros_like(b)
+        nit, _, _ = linear.cg(A, b, x, tol=1e-30, M=M, maxiter=40, check_every=0)
+        assert int(nit.item()) == 40
+        xs.append(x.cpu().numpy())
+    np.testing.assert_array_equal(xs[0], xs[1])

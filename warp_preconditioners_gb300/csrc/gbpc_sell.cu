@@ -528,12 +528,16 @@ constexpr int kDefaultVariant = 4;
 constexpr float kSwitchMargin = 0.90f;
 
 int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
-  if (m.B != 1 || m.nslices == 0) {
+  // Blocked rows: 2 x 2 and 3 x 3 blocks choose between the one-slice
+  // kernel (0) and the pipelined blocked kernel (4); other sizes run 0.
+  const bool blocked = m.B != 1;
+  if (m.nslices == 0 || m.B > 3) {
     m.variant = 0;
     return GBPC_OK;
   }
   // GBPC_SPMV_VARIANT=0..kNumVariants-1 fixes the variant (tests and
-  // tuning); every variant gives the same results.
+  // tuning); every variant gives the same results.  Blocked rows run
+  // variant 4 as the pipelined blocked kernel and 1..3 as 0.
   if (const char* e = std::getenv("GBPC_SPMV_VARIANT")) {
     if (e[0] >= '0' && e[0] <= '9' && e[1] == '\0' && e[0] - '0' < kNumVariants) {
       m.variant = e[0] - '0';
@@ -542,22 +546,27 @@ int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
   }
   // Fewer slices than warps in one grid (kSms CTAs of kThreads): the
   // product is launch-latency-bound and timing the variants measures noise,
-  // so the default stands without the 35 timed launches.
+  // so the default stands without the timed launches.
   if (m.nslices < kSms * (kThreads / 32)) {
-    m.variant = kDefaultVariant;
+    m.variant = blocked ? 0 : kDefaultVariant;
     return GBPC_OK;
   }
   const size_t vs = dtype_size(adtype);
   DevBuf x, z;
   int rc;
-  if ((rc = x.alloc(vs * std::max(m.ncol, 1)))) return rc;
-  if ((rc = z.alloc(vs * std::max(m.nrow, 1)))) return rc;
-  GBPC_CUDA_TRY(cudaMemsetAsync(x.p, 0, vs * std::max(m.ncol, 1), st));
+  // Scalar lengths: nrow and ncol count B x B blocks.
+  const size_t xbytes = vs * (size_t)std::max(m.ncol, 1) * m.B;
+  const size_t zbytes = vs * (size_t)std::max(m.nrow, 1) * m.B;
+  if ((rc = x.alloc(xbytes))) return rc;
+  if ((rc = z.alloc(zbytes))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(x.p, 0, xbytes, st));
   cudaEvent_t e0, e1;
   GBPC_CUDA_TRY(cudaEventCreate(&e0));
   GBPC_CUDA_TRY(cudaEventCreate(&e1));
   float ms[kNumVariants];
   for (int v = 0; v < kNumVariants && !rc; ++v) {
+    ms[v] = 1e30f;
+    if (blocked && v != 0 && v != 4) continue;
     m.variant = v;
     for (int w = 0; w < 2 && !rc; ++w)
       rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);
@@ -572,8 +581,12 @@ int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   int best_v = kDefaultVariant;
-  for (int v = 0; v < kNumVariants && !rc; ++v)
-    if (ms[v] < kSwitchMargin * ms[kDefaultVariant] && ms[v] < ms[best_v]) best_v = v;
+  if (blocked) {
+    best_v = ms[4] < ms[0] ? 4 : 0;
+  } else {
+    for (int v = 0; v < kNumVariants && !rc; ++v)
+      if (ms[v] < kSwitchMargin * ms[kDefaultVariant] && ms[v] < ms[best_v]) best_v = v;
+  }
   m.variant = best_v;
   if (rc) return rc;
   GBPC_CUDA_TRY(cudaGetLastError());

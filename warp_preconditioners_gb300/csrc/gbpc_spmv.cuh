@@ -337,6 +337,115 @@ sell_spmv_pipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A be
   if (DOT) reduce_and_finalize(red, dot_part);
 }
 
+// Blocked rows (B x B blocks), software-pipelined like the scalar kernel
+// above: chunk c + 1's block columns and B*B values are loaded before chunk
+// c's x gathers and FMAs.  The FMAs run in sell_spmv_kernel's order (entry,
+// then block row r, then column q), so the results equal the one-slice
+// blocked kernel's bit for bit.  CH = 2 for 2 x 2 blocks, 1 for 3 x 3 (the
+// 64-register budget).
+template <typename V, int B, int CH>
+__device__ __forceinline__ void load_chunk_b(const SellView<V>& m, const SliceTask& task, int k0,
+                                             int lane, int (&c)[CH], V (&v)[CH][B * B]) {
+  constexpr int BB = B * B;
+  const int32_t* cp = m.cols + task.base + lane;
+  const V* vp = m.vals + task.base * BB + lane;
+#pragma unroll
+  for (int j = 0; j < CH; ++j) {
+    const bool in = k0 + j < task.width;
+    c[j] = in ? __ldg(cp + (int64_t)(k0 + j) * kSlice) : -1;
+#pragma unroll
+    for (int q = 0; q < BB; ++q)
+      v[j][q] = in ? __ldg(vp + ((int64_t)(k0 + j) * BB + q) * kSlice) : static_cast<V>(0.0f);
+  }
+}
+
+template <int B, typename V, typename A, int EPI, bool DOT, int CH, bool UNIT = false>
+__global__ void __launch_bounds__(kThreads, 1)
+sell_spmv_bpipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
+                       const int* guard, EpiDev<A> ep, Reduction red) {
+  constexpr int BB = B * B;
+  const bool run =
+      UNIT || (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = UNIT || (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = UNIT || (flags & F_BETA_ZERO) != 0;
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  const int t = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  // First schedule entries and chunk before the wait (the matrix is not
+  // written while a solve runs; see the scalar kernel).
+  const int64_t idx = sched_index(0, t, warps_total);
+  const bool any = idx < m.nslices;
+  SliceTask cur{-1, 0, 0}, nxt{-1, 0, 0};
+  int pc[CH];
+  V pv[CH][BB];
+  bool have = false;
+  if (any) {
+    cur = load_task(m.sched, idx);
+    const int64_t nidx = sched_index(1, t, warps_total);
+    if (nidx < m.nslices) nxt = load_task(m.sched, nidx);
+    if (run) {
+      load_chunk_b<V, B, CH>(m, cur, 0, lane, pc, pv);
+      have = true;
+    }
+  }
+  pdl_wait();
+  pdl_launch_dependents();
+  if (guard_off(guard)) return;
+  double dot_part = 0.0;
+  if (any) {
+    int i = 0;
+    while (true) {
+      A acc[B];
+#pragma unroll
+      for (int r = 0; r < B; ++r) acc[r] = A(0);
+      if (run) {
+        if (!have) load_chunk_b<V, B, CH>(m, cur, 0, lane, pc, pv);
+        have = false;
+        for (int k0 = 0; k0 < cur.width; k0 += CH) {  // uniform across the warp
+          int c[CH];
+          V v[CH][BB];
+#pragma unroll
+          for (int j = 0; j < CH; ++j) {
+            c[j] = pc[j];
+#pragma unroll
+            for (int q = 0; q < BB; ++q) v[j][q] = pv[j][q];
+          }
+          if (k0 + CH < cur.width) {
+            load_chunk_b<V, B, CH>(m, cur, k0 + CH, lane, pc, pv);
+          } else if (nxt.s >= 0) {
+            load_chunk_b<V, B, CH>(m, nxt, 0, lane, pc, pv);
+            have = true;
+          }
+          A xv[CH][B];
+#pragma unroll
+          for (int j = 0; j < CH; ++j)
+#pragma unroll
+            for (int q = 0; q < B; ++q)
+              xv[j][q] = (c[j] >= 0) ? __ldg(x + (int64_t)c[j] * B + q) : A(0);
+#pragma unroll
+          for (int j = 0; j < CH; ++j) {
+            if (k0 + j < cur.width) {
+#pragma unroll
+              for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int q = 0; q < B; ++q)
+                  acc[r] = fma_t<A>(widen<A, V>(v[j][r * B + q]), xv[j][q], acc[r]);
+            }
+          }
+        }
+      }
+      spmv_finish<B, V, A, EPI, DOT>(m, cur.s * kSlice + lane, acc, y, z, alpha, beta, run,
+                                     alpha_one, beta_zero, ep, red, dot_part);
+      if (nxt.s < 0) break;
+      cur = nxt;
+      ++i;
+      const int64_t nidx = sched_index(i + 1, t, warps_total);
+      nxt = nidx < m.nslices ? load_task(m.sched, nidx) : SliceTask{-1, 0, 0};
+    }
+  }
+  if (DOT) reduce_and_finalize(red, dot_part);
+}
+
 // Launch configuration of a variant: CTAs resident per SM times SMs, with
 // slices spread over the warps by a grid stride.
 // Every variant launches the same grid (one 1024-thread CTA per SM at most),
@@ -419,6 +528,20 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
         return;
       default:
         break;
+    }
+  }
+  if constexpr (B == 2 || B == 3) {
+    if (variant == 4) {
+      constexpr int CH = (B == 2) ? 2 : 1;
+      if (flags == kUnitFlags)
+        launch_k(sell_spmv_bpipe_kernel<B, V, A, EPI, DOT, CH, true>, spmv_grid(nslices, 1),
+                 kThreads, 0, st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags,
+                 guard, e, red);
+      else
+        launch_k(sell_spmv_bpipe_kernel<B, V, A, EPI, DOT, CH>, spmv_grid(nslices, 1), kThreads,
+                 0, st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard,
+                 e, red);
+      return;
     }
   }
   launch_one<B, V, A, EPI, DOT, Chunk<B>::value, 1>(view, x, y, z, alpha, beta, flags, guard, e,
