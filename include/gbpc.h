@@ -133,8 +133,10 @@ int gbpc_fsai_refit(int n, const int32_t* a_off, const int32_t* a_col, const voi
 /* C = A diag(col_scale) B + diag(add_diag), float64 scalar CSR (col_scale,
  * add_diag nullable), on the device: the host SciPy assembly of the
  * smoothing operator Q = alpha M + K M^-1 K (results/dirichlet-tuning/
- * README.md:72-77) with the same summation order (contributions to C_ik in
- * increasing j, then the diagonal term), exact zeros dropped, rows sorted.
+ * README.md:72-77) with SciPy's summation order: with col_scale the
+ * contributions to C_ik arrive in decreasing j (SciPy's intermediate
+ * A diag(d) holds each row with its columns decreasing), without it in
+ * increasing j; then the diagonal term; exact zeros dropped, rows sorted.
  * Two-phase like gbpc_fsai_pack: c_col == NULL fills c_off[nrow+1] and
  * *nnz_host; the second call writes c_col / c_val.  Synchronises. */
 int gbpc_spgemm(int nrow, int ncol, const int32_t* a_off, const int32_t* a_col,
@@ -274,7 +276,10 @@ int gbpc_bsr_transpose(int nrow, int ncol, int block, const int32_t* offsets,
                        int32_t* t_col, void* t_val, void* stream);
 
 /* Apply an operator: z = alpha * Op * x + beta * y (vectors of the
- * operator's vector dtype, length = scalar rows).  Stream-ordered. */
+ * operator's vector dtype, length = scalar rows).  Stream-ordered.  The
+ * LinearOperator `_apply(x, y, z, alpha, beta)` protocol of the reference's
+ * operators (warp_preconditioners/fsai.py:339, :374-381;
+ * sparse_operator.py:90-104; block_ilu.py:188-202). */
 int gbpc_op_apply(gbpc_op* op, const void* x, const void* y, void* z, double alpha, double beta,
                   void* stream);
 
