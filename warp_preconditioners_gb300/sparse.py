@@ -227,9 +227,9 @@ def bsr_mv(a: BsrMatrix, x, y, alpha=1.0, beta=0.0):
 def spgemm(A: BsrMatrix, B: BsrMatrix, col_scale=None, add_diag=None) -> BsrMatrix:
     """``A diag(col_scale) B + diag(add_diag)`` on the device (float64 scalar
     CSR): the host SciPy assembly ``A @ diags(d) @ B + diags(e)`` with the
-    same summation order (over the inner index downwards, as SciPy's
-    intermediate ``A @ diags(d)`` stores its rows), exact zeros dropped and
-    rows sorted."""
+    same summation order (with ``col_scale``, over the inner index downwards,
+    as SciPy's intermediate ``A @ diags(d)`` stores its rows; without it,
+    upwards, as ``A @ B``), exact zeros dropped and rows sorted."""
     import ctypes
 
     from . import _lib
