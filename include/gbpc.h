@@ -320,11 +320,14 @@ int gbpc_krylov(int method, gbpc_op* A, gbpc_op* M, const double* b, double* x, 
  * free of allocation calls (device memory is exhausted or reserved by the
  * host application, or allocation would synchronise or fail mid-pipeline).
  * The intermediate G x lives in a static array inside libgbpc.so of
- * gbpc_fsai_apply_noalloc_max_rows() = 524,288 float64 values (4 MiB), which
- * every GPU that loads the library keeps until the process exits; larger n
- * is rejected with GBPC_ERR_ARG.  The first call on each device looks up
- * that array's device address (cudaGetSymbolAddress), so make the first call
- * on a device before any stream capture.  All calls share the one array:
+ * gbpc_fsai_apply_noalloc_max_rows() = 524,288 float64 values (4 MiB);
+ * larger n is rejected with GBPC_ERR_ARG.  CUDA loads the code holding that
+ * array lazily: the first call on each device loads it and reserves the
+ * 4 MiB there (kept until the process exits), and looks up the array's
+ * device address (cudaGetSymbolAddress).  A call with n == 0 does only this,
+ * so a host that later hands its free memory to a fixed pool makes one such
+ * call per device first; make it, too, before any stream capture.  All calls
+ * share the one array:
  * calls that overlap on the GPU (different streams, no ordering) race and
  * must be avoided.  x, y and z may alias; beta == 0 never reads y and
  * alpha == 0 never reads x.  No cudaMalloc, cudaFree or allocating library

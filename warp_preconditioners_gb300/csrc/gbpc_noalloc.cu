@@ -6,10 +6,12 @@
 // from cudaMalloc, so callers that must not allocate device memory (see the
 // declaration in include/gbpc.h) can still apply the preconditioner.
 //
-// The array is a file-scope __device__ variable: every GPU that loads the
-// library keeps these kNoAllocMaxRows doubles (4 MiB) until the process
-// exits.  Host code only ever passes the array's device address, obtained per
-// device with cudaGetSymbolAddress; the host-side symbol itself is not a
+// The array is a file-scope __device__ variable of kNoAllocMaxRows doubles
+// (4 MiB).  CUDA loads this translation unit's module lazily, so the array is
+// reserved on a device by the first call of gbpc_fsai_apply_noalloc there
+// (a call with n == 0 does only that), and it stays reserved until the
+// process exits.  Host code only ever passes the array's device address,
+// obtained with cudaGetSymbolAddress; the host-side symbol itself is not a
 // device address.
 
 #include <mutex>
@@ -28,17 +30,23 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxRows];
 std::mutex g_scratch_mutex;
 double* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (this is the set-up done by the first call on each device).
-int scratch_address(double** out) {
+// Device address of the scratch array on the current device.  Outside stream
+// capture it is looked up on every call (cheap once the module is loaded, and
+// never stale after a device reset recreated the context); the first lookup
+// on a device loads the module and reserves the array.  Under stream capture
+// the address cached by the last uncaptured call on that device is used, so
+// the first call on each device must come before any capture.
+int scratch_address(cudaStream_t st, double** out) {
   int dev = 0;
   GBPC_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) {
     gbpc_set_error("gbpc_fsai_apply_noalloc: device ordinal %d out of range", dev);
     return GBPC_ERR_ARG;
   }
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  GBPC_CUDA_TRY(cudaStreamIsCapturing(st, &capture));
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (g_scratch_ptr[dev] == nullptr) {
+  if (capture == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) {
@@ -46,6 +54,11 @@ int scratch_address(double** out) {
       return GBPC_ERR_CUDA;
     }
     g_scratch_ptr[dev] = static_cast<double*>(p);
+  } else if (g_scratch_ptr[dev] == nullptr) {
+    gbpc_set_error("gbpc_fsai_apply_noalloc: first call on device %d made under stream "
+                   "capture; call it once (n = 0 is enough) before capturing",
+                   dev);
+    return GBPC_ERR_ARG;
   }
   *out = g_scratch_ptr[dev];
   return GBPC_OK;
@@ -75,7 +88,7 @@ int apply_t(int n, const int32_t* g_off, const int32_t* g_col, const S* g_val,
             const int32_t* gt_off, const int32_t* gt_col, const S* gt_val, const double* x,
             const double* y, double* z, double alpha, double beta, cudaStream_t st) {
   double* tmp = nullptr;
-  int rc = scratch_address(&tmp);
+  int rc = scratch_address(st, &tmp);
   if (rc) return rc;
   const int grid = grid_for(n, kThreads);
   const int alpha_zero = alpha == 0.0;
@@ -108,13 +121,19 @@ extern "C" int gbpc_fsai_apply_noalloc(int n, const int32_t* g_off, const int32_
                    n, kNoAllocMaxRows);
     return GBPC_ERR_ARG;
   }
-  if (n == 0) return GBPC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    // Nothing to compute; the call still reserves the scratch array on the
+    // current device, so a host can make it at start-up, before it takes a
+    // fixed memory pool.
+    double* tmp = nullptr;
+    return scratch_address(st, &tmp);
+  }
   if (!g_off || !g_col || !g_val || !gt_off || !gt_col || !gt_val || !z ||
       (alpha != 0.0 && !x) || (beta != 0.0 && !y)) {
     gbpc_set_error("gbpc_fsai_apply_noalloc: null array argument");
     return GBPC_ERR_ARG;
   }
-  cudaStream_t st = (cudaStream_t)stream;
   if (value_dtype == GBPC_F64)
     return apply_t<double>(n, g_off, g_col, (const double*)g_val, gt_off, gt_col,
                            (const double*)gt_val, x, y, z, alpha, beta, st);
