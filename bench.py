@@ -165,7 +165,8 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def cpu_baseline_sample(prob, width, step_size, method, cpu_iters, iterations_per_rhs):
+def cpu_baseline_sample(prob, width, step_size, method, cpu_iters, iterations_per_rhs,
+                        count_flops=True):
     """Oracle (CPU restatement) on the host cores: FSAI setup + cpu_iters iterations."""
     from oracle import oracle
 
@@ -183,9 +184,39 @@ def cpu_baseline_sample(prob, width, step_size, method, cpu_iters, iterations_pe
     per_iter = (time.perf_counter() - t0) / max(it, 1)
     total = setup + per_iter * sum(iterations_per_rhs)
     # Operation count of the same setup (untimed: the counting run is separate).
-    flops, _, _ = o.fsai_setup_flops(qc, width=width, step=step_size, tol=1e-3)
+    flops = None
+    if count_flops:
+        flops, _, _ = o.fsai_setup_flops(qc, width=width, step=step_size, tol=1e-3)
     return dict(setup_s=setup, per_iteration_s=per_iter, total_s=total, threads=o.num_threads(),
-                iters_sampled=it, setup_flops=flops)
+                iters_sampled=it, setup_flops=flops, factor=(g, gt))
+
+
+def factor_parity(pre, g_or, gt_or):
+    """GPU factor (the one the timed steps built) against the oracle's factor of
+    the same Q: integer arrays compared exactly, values bit for bit and by the
+    largest relative difference."""
+    out = {}
+    for name, dev_m, host in (("G", pre.G, g_or), ("GT", pre.GT, gt_or)):
+        off = dev_m.offsets.cpu().numpy()
+        col = dev_m.columns.cpu().numpy()
+        val = dev_m.values.cpu().numpy()
+        pattern = bool(np.array_equal(off, host.offsets))
+        columns = pattern and bool(np.array_equal(col, host.columns))
+        if columns:
+            same = int(np.count_nonzero(val.view(np.int64) == host.values.view(np.int64)))
+            rel = float(np.max(np.abs(val - host.values) / np.maximum(np.abs(host.values),
+                                                                       np.finfo(float).tiny)))
+        else:
+            same, rel = 0, None
+        out[name] = {"pattern_equal": pattern, "columns_equal": columns, "nnz": int(col.size),
+                     "values_bit_equal": same, "max_rel_diff": rel}
+    out["pattern_equal"] = out["G"]["pattern_equal"] and out["GT"]["pattern_equal"]
+    out["columns_equal"] = out["G"]["columns_equal"] and out["GT"]["columns_equal"]
+    out["max_rel_diff"] = max((out[k]["max_rel_diff"] or 0.0) if out[k]["columns_equal"]
+                              else float("inf") for k in ("G", "GT"))
+    out["bar"] = "pattern and columns exact; values within 1e-12 relative"
+    out["pass"] = bool(out["columns_equal"] and out["max_rel_diff"] <= 1e-12)
+    return out
 
 
 def run_reference(args, prob):
@@ -211,23 +242,30 @@ def run_reference(args, prob):
                                     maxiter=200000)
         full_iters.append(it)
     its = [full_iters[0]] * 4
-    samples = []
+    samples, measured = [], []
     for _ in range(args.steps):
-        s = cpu_baseline_sample(prob, args.width, args.step_size, args.method, args.cpu_iters, its)
+        t0 = time.perf_counter()
+        s = cpu_baseline_sample(prob, args.width, args.step_size, args.method, args.cpu_iters, its,
+                                count_flops=False)
+        measured.append(time.perf_counter() - t0)
         samples.append(s["total_s"])
     t = statistics.median(samples)
     value = 4.0 / t
-    sample = (f"FSAI w{args.width} setup + {args.cpu_iters} PCG iterations of one RHS per step, "
-              f"extrapolated to {full_iters[0]} iterations x 4 RHS (iteration count from one "
-              f"full CPU solve in warm-up)")
+    frac = min(1.0, args.cpu_iters / float(sum(its)))
+    sample = (f"FSAI w{args.width} setup + {args.cpu_iters} PCG iterations of one RHS per step "
+              f"({frac:.1%} of the step's {sum(its)} iterations), extrapolated to "
+              f"{full_iters[0]} iterations x 4 RHS (iteration count from one full CPU solve in "
+              f"warm-up)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args, prob),
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads,
+                         "kind": "port, extrapolated", "sample": sample,
+                         "sampled_fraction": frac,
+                         "measured_ms_per_step": statistics.median(measured) * 1e3},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -424,14 +462,16 @@ def main():
                                  iters[-1])
         line["cpu_baseline"] = {
             "value": 4.0 / cb["total_s"], "unit": "solves/s", "cores": cb["threads"],
-            "kind": "port",
+            "kind": "port, extrapolated",
             "sample": (f"oracle FSAI w{args.width} setup ({cb['setup_s']:.2f} s) + "
                        f"{cb['iters_sampled']} PCG iterations ({cb['per_iteration_s'] * 1e3:.2f} "
                        f"ms each) on one RHS, extrapolated to the GPU's iteration counts "
                        f"{iters[-1]}"),
+            "sampled_fraction": min(1.0, cb["iters_sampled"] / float(sum(iters[-1]))),
         }
         line["fsai_setup_roofline"] = fsai_setup_roofline(cb["setup_flops"],
                                                           line["refit"]["setup_ms"])
+        line["parity"] = factor_parity(pre, *cb["factor"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

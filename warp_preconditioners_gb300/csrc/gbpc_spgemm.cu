@@ -164,13 +164,21 @@ extern "C" int gbpc_spgemm(int nrow, int ncol, const int32_t* a_off, const int32
   GBPC_CUDA_TRY(cudaStreamSynchronize(st));
   // Distinct columns of a row of C never exceed maxA * maxB (+1 diagonal).
   const int64_t bound = (int64_t)h[0] * h[1] + 1;
-  int H = 64, hbits = 6;
-  while (H < 2 * bound) { H <<= 1; ++hbits; }
   int smem_optin = 0, dev = 0;
   GBPC_CUDA_TRY(cudaGetDevice(&dev));
   GBPC_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t smem = (size_t)kSgWarps * (H + H / 2) * (sizeof(double) + sizeof(int));
-  if (smem > (size_t)smem_optin) {
+  // Table sizes are powers of two from 64 up; the largest one that fits the
+  // opt-in shared memory ends the search, so H never overflows.
+  int64_t H64 = 64;
+  int hbits = 6;
+  while (H64 < 2 * bound &&
+         (size_t)kSgWarps * (H64 + H64 / 2) * (sizeof(double) + sizeof(int)) <= (size_t)smem_optin) {
+    H64 <<= 1;
+    ++hbits;
+  }
+  const size_t smem = (size_t)kSgWarps * (H64 + H64 / 2) * (sizeof(double) + sizeof(int));
+  const int H = (int)std::min<int64_t>(H64, 1 << 30);
+  if (H64 < 2 * bound || smem > (size_t)smem_optin) {
     gbpc_set_error("gbpc_spgemm: rows too long (%lld candidate columns per row)", (long long)bound);
     return GBPC_ERR_UNSUPPORTED;
   }
