@@ -81,12 +81,16 @@ void fsai_diagonal(int n, const int32_t* off, const int32_t* col, const T* val, 
 // with the lookup's zero: it is not counted, since it contributes nothing
 // and a sparse implementation skips it; the small dense Cholesky updates are
 // counted in full.
+//
+// The row's width slots are written at output row `out_row` (row i itself
+// when every row is built; its position in the list when only some are).
 template <typename T, bool COUNT = false>
 void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val, const T* scale,
                     T tolerance, T pivot_floor, int width, int step, int32_t* cols_out,
                     T* vals_out, int& truncated, int& invalid, std::vector<int>& pattern,
                     std::vector<T>& chol, std::vector<T>& z, std::vector<T>& v, std::vector<T>& w,
-                    std::vector<int>& cand, std::vector<T>& sc, int64_t& flops) {
+                    std::vector<int>& cand, std::vector<T>& sc, int64_t& flops, int out_row = -1) {
+  if (out_row < 0) out_row = i;
   std::fill(pattern.begin(), pattern.end(), -1);
   std::fill(chol.begin(), chol.end(), T(0));
   std::fill(z.begin(), z.end(), T(0));
@@ -195,7 +199,7 @@ void fsai_build_row(int i, const int32_t* off, const int32_t* col, const T* val,
   if constexpr (COUNT) flops += 1 + 2 * (int64_t)size;
   bool valid = true;
   for (int p = 0; p < width; ++p) {
-    const size_t e = (size_t)i * width + p;
+    const size_t e = (size_t)out_row * width + p;
     cols_out[e] = -1;
     vals_out[e] = T(0);
     if (p < size) {
@@ -228,6 +232,32 @@ void fsai_setup(int n, const int32_t* off, const int32_t* col, const T* val, int
   status[1] += truncated;
   status[2] += invalid;
   if (flops_out) *flops_out = flops;
+}
+
+// The same build for the listed rows only (every row of the reference's
+// build is independent, so any subset gives exactly those rows of the full
+// factor): row rows[k] is written to output row k.  Scales are computed for
+// all rows, since a row's scores read its candidates' scales.
+template <typename T>
+void fsai_setup_rows(int n, const int32_t* off, const int32_t* col, const T* val, int width,
+                     int step, T tolerance, T pivot_floor, int nrows, const int32_t* rows,
+                     int32_t* cols_out, T* vals_out, int32_t* status) {
+  std::vector<T> scale((size_t)std::max(n, 1));
+  fsai_diagonal(n, off, col, val, scale.data(), status);
+  int truncated = 0, invalid = 0;
+  int64_t flops = 0;
+#pragma omp parallel reduction(+ : truncated, invalid)
+  {
+    std::vector<int> pattern(width), cand(step);
+    std::vector<T> chol((size_t)width * width), z(width), v(width), w(width), sc(step);
+#pragma omp for schedule(dynamic, 16)
+    for (int k = 0; k < nrows; ++k)
+      fsai_build_row<T, false>(rows[k], off, col, val, scale.data(), tolerance, pivot_floor,
+                               width, step, cols_out, vals_out, truncated, invalid, pattern,
+                               chol, z, v, w, cand, sc, flops, k);
+  }
+  status[1] += truncated;
+  status[2] += invalid;
 }
 
 // warp_preconditioners/fsai_pack.py:15-71 (`sort_rows`, `array_scan`, `pack`).
@@ -1087,6 +1117,13 @@ void or_fsai_setup_f64(int n, const int32_t* off, const int32_t* col, const doub
                        int width, int step, double tol, double floor_, int32_t* cols_out,
                        double* vals_out, double* scale, int32_t* status) {
   fsai_setup<double>(n, off, col, val, width, step, tol, floor_, cols_out, vals_out, scale, status);
+}
+void or_fsai_setup_rows_f64(int n, const int32_t* off, const int32_t* col, const double* val,
+                            int width, int step, double tol, double floor_, int nrows,
+                            const int32_t* rows, int32_t* cols_out, double* vals_out,
+                            int32_t* status) {
+  fsai_setup_rows<double>(n, off, col, val, width, step, tol, floor_, nrows, rows, cols_out,
+                          vals_out, status);
 }
 // FSAI setup that also counts its floating-point operations.
 int64_t or_fsai_setup_flops_f64(int n, const int32_t* off, const int32_t* col, const double* val,

@@ -122,6 +122,30 @@ def fsai_setup(a: CSR, width=8, step=1, tol=1e-3, pivot_floor=None):
     return cols, vals, scale, status
 
 
+def fsai_rows(a: CSR, rows, width=8, step=1, tol=1e-3, pivot_floor=None):
+    """The float64 FSAI rows `rows` only (fsai.py:60-176 builds every row
+    independently): returns (columns, values) per listed row, each sorted by
+    column like the packed factor (fsai_pack.py:15-71), and status[3]."""
+    a = CSR(a.offsets, a.columns, np.ascontiguousarray(a.values, np.float64), a.ncol)
+    if pivot_floor is None:
+        pivot_floor = 1e-12
+    rows = np.ascontiguousarray(rows, np.int32)
+    cols = np.empty(max(len(rows), 1) * width, np.int32)
+    vals = np.empty(max(len(rows), 1) * width, np.float64)
+    status = np.zeros(3, np.int32)
+    lib().or_fsai_setup_rows_f64(a.nrow, _p(a.offsets), _p(a.columns), _p(a.values), width, step,
+                                 ctypes.c_double(tol), ctypes.c_double(pivot_floor), len(rows),
+                                 _p(rows), _p(cols), _p(vals), _p(status))
+    out = []
+    for k in range(len(rows)):
+        c = cols[k * width:(k + 1) * width]
+        v = vals[k * width:(k + 1) * width]
+        keep = c >= 0
+        order = np.argsort(c[keep], kind="stable")
+        out.append((c[keep][order], v[keep][order]))
+    return out, status
+
+
 def fsai_setup_flops(a: CSR, width=8, step=1, tol=1e-3, pivot_floor=None):
     """Floating-point operations of the float64 FSAI setup (fsai.py:44-176),
     counted while the oracle runs it: each separately rounded multiply,
