@@ -116,8 +116,10 @@ def test_block_jacobi_and_ilu0_at_64cubed(oracle, coupling64):
     ilu.matvec(vec(x_np), vec(np.zeros_like(x_np)), z, 1.0, 0.0)
     want = oracle.bilu0_apply(nrow, 3, bsr.indptr, bsr.indices, fac, inv2, 3, x_np,
                               np.zeros_like(x_np), 1.0, 0.0)
-    np.testing.assert_allclose(z.cpu().numpy(), want, rtol=1e-12,
-                               atol=1e-12 * np.abs(want).max())
+    # 1e-9 of the largest entry: the 1e6-conditioned 3 x 3 inverse blocks
+    # amplify the fused multiply-adds' rounding differences.
+    np.testing.assert_allclose(z.cpu().numpy(), want, rtol=1e-9,
+                               atol=1e-9 * np.abs(want).max())
 
 
 def test_scalarised_fsai_at_64cubed(oracle, coupling64):

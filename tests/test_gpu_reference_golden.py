@@ -6,8 +6,10 @@ tests/golden/make_reference_golden.py).  Integer arrays (FSAI supports,
 transposes) must be equal, and so must the values: the setup kernels follow
 the reference's operation order without contraction, so FSAI, refit, block
 Jacobi, block ILU(0) and block FSAI factors are compared bit for bit.
-Products (FSAI apply, factored operator, ILU apply) are compared at 1e-12
-relative, since the device sums rows in its own order.
+Products (FSAI apply, factored operator) are compared at 1e-12 relative,
+since the device sums rows in its own order with fused multiply-adds; the
+block applies at 1e-9 of the largest entry (their inverse blocks carry a
+1e6 condition number).
 """
 
 import numpy as np
@@ -108,11 +110,15 @@ def test_block_jacobi_and_ilu0(ref_block):
                                   _bits(ref_block["kron6_ilu_factors"]))
     np.testing.assert_array_equal(_bits(ilu.inverse_diagonal.cpu().numpy()),
                                   _bits(ref_block["kron6_ilu_inverse"]))
+    # The applies multiply by inverse blocks of C = R diag(1, 1, 1e-6) R^T,
+    # whose 1e6 condition number turns the device's fused multiply-adds
+    # (one rounding fewer per product than the reference) into relative
+    # differences up to ~1e-10: 1e-9 of the largest entry is the bar here.
     x, y = vec(ref_block["kron6_x"]), vec(ref_block["kron6_y"])
     for op, key in ((ilu, "kron6_ilu_apply"), (jac, "kron6_jacobi_apply")):
         z = torch.empty_like(x)
         op.matvec(x, y, z, 0.7, -0.2)
-        _close(z.cpu().numpy(), ref_block[key])
+        _close(z.cpu().numpy(), ref_block[key], rtol=1e-9)
 
 
 def test_scalarised_and_block_fsai(ref_block):
