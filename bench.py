@@ -453,6 +453,8 @@ def main():
         line["mixed_batched"] = run_mixed_batched(args, prob, Q, K, mass, free, dev)
     if not args.no_mixed:
         line["batched_rhs4"] = measure_batched_rhs4(args, prob, Q, K, mass, dev, ms_per_step)
+        line["f32_apply_rhs4"] = measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev,
+                                                        ms_per_step)
     line["refit"] = measure_refit(args, prob, Q, dev)
     line["assembly"] = measure_assembly(prob, dev)
     if args.lifted:
@@ -551,6 +553,15 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
         nit, _ = bs.solve(B, X, tol=args.rtol, maxiter=100000)
         return X, nit.clone()
 
+    def batch_f32m(factor_dtype):
+        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3,
+                   apply_dtype=torch.float32, factor_dtype=factor_dtype)
+        bs = batched.BatchedSolver(K, mass, ALPHA, pre, factor_dtype=factor_dtype,
+                                   apply_dtype=torch.float32)
+        X = torch.zeros_like(B)
+        nit, _ = bs.solve(B, X, tol=args.rtol, maxiter=100000)
+        return X, nit.clone()
+
     def mixed():
         pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
         ms = batched.MixedPrecisionSolver(K, mass, ALPHA, pre, torch.bfloat16)
@@ -569,8 +580,10 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
         return e0.elapsed_time(e1), out
 
     batch64()  # warm-up (graph capture paths)
+    batch_f32m(torch.bfloat16)
     t_plain, (xs, its) = timed(plain)
     t_batch, (Xb, nitb) = timed(batch64)
+    low = {dt: timed(lambda: batch_f32m(dt)) for dt in (torch.bfloat16, torch.float32)}
     if args.fp32_refinement:
         t_mixed, (Xm, outer, inner) = timed(mixed)
     qh = prob["Q"]
@@ -599,6 +612,16 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             "iterations_max": int(nitb.max().item()), "backward_error_max": berr_b,
             "rel_diff_vs_plain_max": rel_b},
     }
+    for dt, (t_low, (Xl, nitl)) in low.items():
+        berr_l, rel_l = quality(Xl.cpu().numpy())
+        name = "bf16" if dt == torch.bfloat16 else "f32"
+        out[f"batched_f32_apply_{name}"] = {
+            "solver": (f"one batched float64 PCG for all {k} RHS with the FSAI factor stored in "
+                       f"{name} and applied in float32 (float64 operator, recurrences and dots)"),
+            "ms": t_low, "solves_per_s": k / (t_low / 1e3), "speedup": t_plain / t_low,
+            "speedup_vs_batched_fp64": t_batch / t_low,
+            "iterations_max": int(nitl.max().item()), "backward_error_max": berr_l,
+            "rel_diff_vs_plain_max": rel_l}
     if args.fp32_refinement:
         berr_m, rel_m = quality(Xm.cpu().numpy())
         out["float32_refinement"] = {
@@ -607,6 +630,61 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             "ms": t_mixed, "speedup": t_plain / t_mixed, "outer_max": int(max(outer)),
             "inner_max": int(max(inner)), "backward_error_max": berr_m,
             "rel_diff_vs_plain_max": rel_m}
+    return out
+
+
+def measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev, ms_per_step):
+    """The default step (setup + 4 sequential CG solves through linear.Solver)
+    with the FSAI factor applied in float32 (stored in bfloat16 or float32),
+    everything else float64; CUDA-event medians of 3 steps."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, linear
+
+    n = prob["n"]
+    rhs = torch.as_tensor(prob["rhs"], device=dev).contiguous()
+    b = torch.empty(n, dtype=torch.float64, device=dev)
+    out = {}
+    for dt in (torch.bfloat16, torch.float32):
+        xs = torch.zeros((4, n), dtype=torch.float64, device=dev)
+
+        def step():
+            op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
+            pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
+                       kap_tolerance=1e-3, apply_dtype=torch.float32, factor_dtype=dt)
+            solver = linear.Solver(args.method, op, pre)
+            its = []
+            for j in range(4):
+                b.copy_(rhs[j])
+                xs[j].zero_()
+                nit, _, _ = solver.run(b, xs[j], tol=args.rtol, maxiter=100000)
+                its.append(nit.clone())
+            return its
+
+        step()
+        times = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            its = step()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        t = statistics.median(times)
+        qh = prob["Q"]
+        sols = xs.cpu().numpy()
+        absq = abs(qh)
+        berr = [float(np.max(np.abs(prob["rhs"][j] - qh @ sols[j])
+                             / (absq @ np.abs(sols[j]) + np.abs(prob["rhs"][j]))))
+                for j in range(4)]
+        name = "bf16" if dt == torch.bfloat16 else "f32"
+        out[name] = {"ms_per_step": t, "solves_per_s": 4e3 / t,
+                     "speedup_vs_drop_in": ms_per_step / t,
+                     "iterations": [int(i.item()) for i in its], "backward_error_max": max(berr)}
+    out["solver"] = ("the default step (setup + 4 sequential CG solves) with FSAI(..., "
+                     "apply_dtype=torch.float32): factor stored in bf16 / f32 and applied in "
+                     "float32; operator, recurrences and dots float64")
     return out
 
 

@@ -53,6 +53,14 @@ enum gbpc_status {
 
 enum gbpc_dtype { GBPC_F64 = 0, GBPC_F32 = 1, GBPC_BF16 = 2 };
 
+/* Vector dtype code of a preconditioner applied in float32 behind a float64
+ * interface: x, y, z are float64, the operator converts x to float32, runs
+ * its products with float32 arithmetic on float32 or bfloat16 storage, and
+ * widens the result (the precision option of the preconditioner only; the
+ * Krylov method and the system operator stay float64).  Inside gbpc_solver
+ * (CG) the conversions are fused into the loop's own vector kernels. */
+enum { GBPC_F32_APPLY = 3 };
+
 enum gbpc_method { GBPC_CG = 0, GBPC_CR = 1 };
 
 /* Message of the last failing call on this thread (never NULL). */
@@ -186,7 +194,10 @@ int gbpc_op_shifted_block(int order, int n, double scale, int dtype, gbpc_op* hi
 /* Gram-form approximate inverse z = alpha * G^T (G x) + beta * y from
  * explicit G and G^T (scalar CSR, or b x b BSR for block FSAI).  Replaces
  * FSAI._apply (warp_preconditioners/fsai.py:393-400) and BsrBlockFSAI._apply
- * (benchmarks/block_fsai_candidate.py:311-332). */
+ * (benchmarks/block_fsai_candidate.py:311-332).  vector_dtype F64 / F32, or
+ * GBPC_F32_APPLY (value_dtype F32 or BF16) for float64 vectors with float32
+ * arithmetic inside; the reference's float32 factor storage
+ * (fsai.py:255-263) accumulates in float64, which is vector_dtype F64. */
 int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int32_t* g_col,
                  const void* g_val, const int32_t* gt_off, const int32_t* gt_col,
                  const void* gt_val, int value_dtype, int vector_dtype, void* stream,

@@ -17,6 +17,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libgbpc.so"
 
 GBPC_F64, GBPC_F32, GBPC_BF16 = 0, 1, 2
+GBPC_F32_APPLY = 3  # float64 vectors, float32 arithmetic inside (preconditioners)
 GBPC_CG, GBPC_CR = 0, 1
 
 OK = 0

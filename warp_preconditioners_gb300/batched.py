@@ -114,6 +114,7 @@ class BatchedCG:
     """k independent PCG recurrences on one operator, per-RHS stopping."""
 
     def __init__(self, A: BatchedOperator, M: BatchedOperator, unroll=0, max_rhs=None):
+        # M may be float32 behind a float64 A (float32-applied preconditioner).
         self.A, self.M = A, M
         self.max_rhs = _max_rhs(max_rhs if max_rhs is not None else min(A.max_rhs, M.max_rhs))
         out = ctypes.c_void_p()
@@ -160,12 +161,25 @@ def refine(A64: BatchedOperator, inner: BatchedCG, B, X, tol_outer=1e-12, tol_in
 class BatchedSolver:
     """k right-hand sides of the factored smoothing system in one float64
     batched PCG (float64 operator and vectors; `factor_dtype` stores the FSAI
-    factor).  Matrix bytes are read once per iteration for the whole batch."""
+    factor).  Matrix bytes are read once per iteration for the whole batch.
+
+    ``apply_dtype=torch.float32`` applies the preconditioner with float32
+    arithmetic (factor stored in ``factor_dtype``, float32 or bfloat16): the
+    update kernel hands it a float32 copy of the residual and the direction
+    update widens its output, while the operator, the recurrences and every
+    dot product stay float64."""
 
     def __init__(self, L: BsrMatrix, mass: torch.Tensor, mass_weight: float, pre: FSAI,
-                 factor_dtype=torch.float64, unroll=0):
+                 factor_dtype=torch.float64, unroll=0, apply_dtype=None):
         self.A = batched_sqlap(L, mass, mass_weight, torch.float64, torch.float64)
-        self.M = batched_fsai(pre, factor_dtype, torch.float64)
+        if apply_dtype == torch.float32:
+            if factor_dtype not in (torch.float32, torch.bfloat16):
+                raise ValueError("a float32 apply needs float32 or bfloat16 factor storage")
+            self.M = batched_fsai(pre, factor_dtype, torch.float32)
+        elif apply_dtype in (None, torch.float64):
+            self.M = batched_fsai(pre, factor_dtype, torch.float64)
+        else:
+            raise ValueError("apply_dtype must be torch.float64 or torch.float32")
         self.cg = BatchedCG(self.A, self.M, unroll)
 
     def solve(self, B, X, tol=1e-8, atol=0.0, maxiter=0):

@@ -61,6 +61,7 @@ struct BRed {
   int mode;
   BatchScalars* bs;
   double* out;
+  int w_f64;         // w is float64 although out is float32 (float32 preconditioner)
 };
 
 template <typename T> __device__ __forceinline__ T fma_bt(T a, T b, T c);
@@ -318,7 +319,12 @@ bspmm_kernel(int nrow, int k, const int32_t* __restrict__ off, const int32_t* __
       }
       if (!beta_zero) out = fma_bt<T>((T)beta, Y[idx], out);
       Z[idx] = out;
-      if (DOT) dot = fma((double)out, (double)((const T*)red.w)[idx], dot);
+      if (DOT) {
+        const double wv = (!std::is_same<T, double>::value && red.w_f64)
+                              ? ((const double*)red.w)[idx]
+                              : (double)((const T*)red.w)[idx];
+        dot = fma((double)out, wv, dot);
+      }
     }
   }
   if (DOT) b_reduce(red, b_fold<KP>(dot));
@@ -349,10 +355,13 @@ bdot_kernel(int64_t n, int k, const T* a, const T* b, BRed red) {
   b_reduce(red, b_fold<KP>(s));
 }
 
-// X += alpha_j P; R -= alpha_j AP; reduce r.r  (inactive RHS untouched)
+// X += alpha_j P; R -= alpha_j AP; reduce r.r  (inactive RHS untouched).
+// R32 != nullptr: also R32 = (float) R, the input of a float32
+// preconditioner inside the float64 loop.
 template <typename T, int KP>
 __global__ void __launch_bounds__(kBThreads)
-bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, const T* AP, BRed red) {
+bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, const T* AP,
+                  float* R32, BRed red) {
   pdl_wait();
   pdl_launch_dependents();
   if (*(volatile int*)&bs->any_active == 0) return;
@@ -371,16 +380,17 @@ bcg_update_kernel(int64_t n, int k, BatchScalars* bs, T* X, T* R, const T* P, co
         X[idx] = fma_bt<T>(a, P[idx], X[idx]);
         r = fma_bt<T>(-a, AP[idx], r);
         R[idx] = r;
+        if (R32) R32[idx] = (float)r;
       }
       s = fma((double)r, (double)r, s);
     }
   b_reduce(red, b_fold<KP>(s));
 }
 
-// P = Z + beta_j P  (active RHS only)
-template <typename T, int KP>
+// P = Z + beta_j P  (active RHS only); Z may be float32 (widened).
+template <typename T, int KP, typename ZT = T>
 __global__ void __launch_bounds__(kBThreads)
-bxpay_kernel(int64_t n, int k, const BatchScalars* bs, const T* Zv, T* P) {
+bxpay_kernel(int64_t n, int k, const BatchScalars* bs, const ZT* Zv, T* P) {
   pdl_wait();
   pdl_launch_dependents();
   if (*(volatile const int*)&bs->any_active == 0) return;
@@ -392,7 +402,7 @@ bxpay_kernel(int64_t n, int k, const BatchScalars* bs, const T* Zv, T* P) {
     const int64_t row = wb * GR + grp;
     if (row >= n) continue;
     const int64_t idx = row * k + j;
-    P[idx] = fma_bt<T>(b, P[idx], Zv[idx]);
+    P[idx] = fma_bt<T>(b, P[idx], (T)Zv[idx]);
   }
 }
 
@@ -671,7 +681,11 @@ struct BSolver {
   int64_t n = 0;
   int vdtype = GBPC_F32;
   int max_rhs = kB;
-  DevBuf R, Zv, P, AP, bs, partials, counter;
+  // Float64 loop with a float32 preconditioner (A float64, M float32): the
+  // update kernel writes R32, M maps R32 to Z32 with the float64 dot r.z,
+  // and the direction update widens Z32.
+  bool mixed_m = false;
+  DevBuf R, Zv, P, AP, bs, partials, counter, R32, Z32;
   // Graph being built (moved into `graphs` once instantiated).
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
@@ -730,6 +744,18 @@ struct BSolver {
     BRed rrr = red(R.p, BF_INIT_RR);
     if ((rc = A->apply(k, X, B, R.p, -1.0, 1.0, nullptr, &rrr, st))) return rc;
     BRed rrz = red(R.p, BF_INIT_RZ);
+    if (mixed_m) {
+      const int64_t count = n * k;
+      convert_kernel<float, double><<<e_grid(count), 256, 0, st>>>(count, R.as<double>(),
+                                                                   R32.as<float>());
+      GBPC_CUDA_TRY(cudaGetLastError());
+      rrz.w_f64 = 1;
+      if ((rc = M->apply(k, R32.p, nullptr, Z32.p, 1.0, 0.0, nullptr, &rrz, st))) return rc;
+      convert_kernel<double, float><<<e_grid(count), 256, 0, st>>>(count, Z32.as<float>(),
+                                                                   P.as<double>());
+      GBPC_CUDA_TRY(cudaGetLastError());
+      return GBPC_OK;
+    }
     if ((rc = M->apply(k, R.p, nullptr, Zv.p, 1.0, 0.0, nullptr, &rrz, st))) return rc;
     GBPC_CUDA_TRY(cudaMemcpyAsync(P.p, Zv.p, vbytes(k), cudaMemcpyDeviceToDevice, st));
     return GBPC_OK;
@@ -742,13 +768,25 @@ struct BSolver {
     BRed ra = red(P.p, BF_ALPHA);
     if ((rc = A->apply(k, P.p, nullptr, AP.p, 1.0, 0.0, guard, &ra, st))) return rc;
     BRed rr = red(R.p, BF_RR);
+    float* r32 = mixed_m ? R32.as<float>() : nullptr;
     with_kp(k, [&](auto kpc) {
       constexpr int KP = decltype(kpc)::value;
       launch_k(bcg_update_kernel<T, KP>, b_grid(n, KP), kBThreads, 0, st, n, k, S(), (T*)X,
-               (T*)R.p, (const T*)P.p, (const T*)AP.p, rr);
+               (T*)R.p, (const T*)P.p, (const T*)AP.p, r32, rr);
     });
     GBPC_CUDA_TRY(cudaGetLastError());
     BRed rb = red(R.p, BF_BETA);
+    if (mixed_m) {
+      rb.w_f64 = 1;
+      if ((rc = M->apply(k, R32.p, nullptr, Z32.p, 1.0, 0.0, guard, &rb, st))) return rc;
+      with_kp(k, [&](auto kpc) {
+        constexpr int KP = decltype(kpc)::value;
+        launch_k(bxpay_kernel<T, KP, float>, b_grid(n, KP), kBThreads, 0, st, n, k,
+                 (const BatchScalars*)S(), (const float*)Z32.p, (T*)P.p);
+      });
+      GBPC_CUDA_TRY(cudaGetLastError());
+      return GBPC_OK;
+    }
     if ((rc = M->apply(k, R.p, nullptr, Zv.p, 1.0, 0.0, guard, &rb, st))) return rc;
     with_kp(k, [&](auto kpc) {
       constexpr int KP = decltype(kpc)::value;
@@ -1038,9 +1076,13 @@ extern "C" int gbpc_bop_destroy(gbpc_bop* op) {
 
 extern "C" int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, int max_rhs,
                                    void* stream, gbpc_bsolver** out) {
-  if (!out || !A || !M || A->impl->rows != M->impl->rows || A->impl->vdtype != M->impl->vdtype) {
+  // Vector dtypes: equal, or a float64 operator with a float32 preconditioner
+  // (the loop stays float64; only M runs in float32).
+  const bool mixed_m = A && M && A->impl->vdtype == GBPC_F64 && M->impl->vdtype == GBPC_F32;
+  if (!out || !A || !M || A->impl->rows != M->impl->rows ||
+      (A->impl->vdtype != M->impl->vdtype && !mixed_m)) {
     gbpc_set_error("gbpc_bsolver_create: operator and preconditioner must match in size and "
-                   "vector dtype");
+                   "vector dtype (or pair a float64 operator with a float32 preconditioner)");
     return GBPC_ERR_ARG;
   }
   if (max_rhs < 1 || max_rhs > kB) {
@@ -1061,6 +1103,9 @@ extern "C" int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, int max
   if (!rc) rc = s.Zv.alloc(bytes);
   if (!rc) rc = s.P.alloc(bytes);
   if (!rc) rc = s.AP.alloc(bytes);
+  s.mixed_m = mixed_m;
+  if (!rc && mixed_m) rc = s.R32.alloc(sizeof(float) * std::max<int64_t>(s.n, 1) * max_rhs);
+  if (!rc && mixed_m) rc = s.Z32.alloc(sizeof(float) * std::max<int64_t>(s.n, 1) * max_rhs);
   if (!rc) rc = s.bs.alloc(sizeof(BatchScalars));
   if (!rc) rc = s.partials.alloc(sizeof(double) * kBMaxCtas * kB);
   if (!rc) rc = s.counter.alloc(sizeof(unsigned int));

@@ -164,6 +164,19 @@ struct Operator {
   DevBuf alias_scratch;  // copy of x when x aliases z
 };
 
+// A preconditioner applied in float32 behind a float64 interface
+// (GBPC_F32_APPLY): apply() narrows x into in32, runs `inner` (float32
+// vectors) into out32 and widens alpha * out32 + beta * y into z with the
+// fused dot.  The CG solver writes in32 and reads out32 itself, so inside
+// its loop only `inner` runs.
+struct LowPrecisionOp : Operator {
+  std::unique_ptr<Operator> inner;
+  DevBuf in32, out32;
+  int apply(const void* x, const void* y, void* z, double alpha, double beta, const int* guard,
+            const DotSpec* dot, cudaStream_t st) override;
+  bool gathers_x() const override { return false; }
+};
+
 }  // namespace gbpc
 
 struct gbpc_op {

@@ -35,10 +35,12 @@ __device__ __forceinline__ bool inactive(const KrylovScalars* ks) {
   return *(volatile const int*)&ks->active == 0;
 }
 
-// x += alpha p; r -= alpha Ap; reduce r.r
+// x += alpha p; r -= alpha Ap; reduce r.r.  R32: also r32 = (float) r, the
+// input of a float32-applied preconditioner (no separate conversion pass).
+template <bool R32>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const double* p,
-                 const double* Ap, Reduction red) {
+                 const double* Ap, float* r32, Reduction red) {
   // x and p are not written by the previous kernel (the operator apply that
   // produced Ap), so a thread's first row of them is read before the wait.
   const int64_t i0 = (int64_t)blockIdx.x * kThreads + threadIdx.x;
@@ -57,6 +59,7 @@ cg_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, const doubl
     x[i] = fma(alpha, first ? p0 : p[i], first ? x0 : x[i]);
     const double ri = fma(-alpha, Ap[i], r[i]);
     r[i] = ri;
+    if (R32) r32[i] = (float)ri;
     part = fma(ri, ri, part);
   }
   reduce_and_finalize(red, part);
@@ -83,10 +86,11 @@ cr_update_kernel(int64_t n, KrylovScalars* ks, double* x, double* r, double* z, 
 }
 
 // p = z + beta p  (and q = w + beta q with Q: CR).  Q is a template
-// parameter so that CG issues no FP64 instruction for the absent q.
-template <bool Q>
+// parameter so that CG issues no FP64 instruction for the absent q.  Z is
+// float for a float32-applied preconditioner (z widened on the fly).
+template <bool Q, typename Z = double>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
-xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, const double* w,
+xpay_kernel(int64_t n, const KrylovScalars* ks, const Z* z, double* p, const double* w,
             double* q) {
   // p (and q) were last written an iteration ago, not by the previous
   // kernel: a thread's first row of them is read before the wait.
@@ -102,7 +106,7 @@ xpay_kernel(int64_t n, const KrylovScalars* ks, const double* z, double* p, cons
   const double beta = ks->beta;
   for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * kThreads) {
     const bool first = i == i0;
-    p[i] = fma(beta, first ? p0 : p[i], z[i]);
+    p[i] = fma(beta, first ? p0 : p[i], (double)z[i]);
     if (Q) q[i] = fma(beta, first ? q0 : q[i], w[i]);
   }
 }
@@ -115,6 +119,20 @@ dot_kernel(int64_t n, const double* a, const double* b, Reduction red) {
        i += (int64_t)gridDim.x * kThreads)
     part = fma(a[i], b[i], part);
   reduce_and_finalize(red, part);
+}
+
+// r32 = (float) r (initialisation of the float32-preconditioned loop).
+__global__ void narrow_copy_kernel(int64_t n, const double* r, float* r32) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r32[i] = (float)r[i];
+}
+
+// p = (double) z32.
+__global__ void widen_copy_kernel(int64_t n, const float* z32, double* p) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = (double)z32[i];
 }
 
 __global__ void set_scalars_kernel(KrylovScalars* ks, double tol, double atol, int maxiter,
@@ -143,6 +161,11 @@ struct Solver {
   int method = GBPC_CG;
   Operator* A = nullptr;
   Operator* M = nullptr;
+  // M applied in float32 behind a float64 interface: CG writes its float32
+  // input (low->in32) in the update kernel and reads its float32 output
+  // (low->out32) in the direction update, so only low->inner runs per
+  // iteration (CR uses M's own float64 interface).
+  LowPrecisionOp* low = nullptr;
   int64_t n = 0;
   bool use_graph = true;
   int unroll = 8;  // iterations per pass of the device loop (measured: 1 -> 8 saves ~4 us/iteration)
@@ -209,7 +232,15 @@ struct Solver {
     if ((rc = A->apply(x, b, r.p, -1.0, 1.0, nullptr, &drr, st))) return rc;
     // z = M r, rz = r.z   (set_active already ran; inactive solves still
     // compute these harmless initial quantities).
-    if (method == GBPC_CG) {
+    if (method == GBPC_CG && low) {
+      DotSpec drz = dot(r.as<double>(), FIN_INIT_RZ);
+      narrow_copy_kernel<<<vec_grid(n), kThreads, 0, st>>>(n, r.as<double>(), low->in32.as<float>());
+      GBPC_CUDA_TRY(cudaGetLastError());
+      if ((rc = low->inner->apply(low->in32.p, nullptr, low->out32.p, 1.0, 0.0, nullptr, &drz, st)))
+        return rc;
+      widen_copy_kernel<<<vec_grid(n), kThreads, 0, st>>>(n, low->out32.as<float>(), p.as<double>());
+      GBPC_CUDA_TRY(cudaGetLastError());
+    } else if (method == GBPC_CG) {
       DotSpec drz = dot(r.as<double>(), FIN_INIT_RZ);
       if ((rc = precondition(r.as<double>(), z.as<double>(), nullptr, &drz, st))) return rc;
       GBPC_CUDA_TRY(cudaMemcpyAsync(p.p, z.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -232,12 +263,24 @@ struct Solver {
     rrr.mode = FIN_RR;
     rrr.ks = K();
     rrr.w = r.as<double>();
-    if (method == GBPC_CG) {
+    if (method == GBPC_CG && low) {
       DotSpec da = dot(p.as<double>(), FIN_CG_ALPHA);
       if ((rc = A->apply(p.p, nullptr, Ap.p, 1.0, 0.0, guard, &da, st))) return rc;
-      GBPC_CUDA_TRY(launch_k(cg_update_kernel, vec_grid(n), kThreads, 0, st, n, K(), x,
+      GBPC_CUDA_TRY(launch_k(cg_update_kernel<true>, vec_grid(n), kThreads, 0, st, n, K(), x,
                              r.as<double>(), (const double*)p.as<double>(),
-                             (const double*)Ap.as<double>(), rrr));
+                             (const double*)Ap.as<double>(), low->in32.as<float>(), rrr));
+      DotSpec db = dot(r.as<double>(), FIN_CG_BETA);
+      if ((rc = low->inner->apply(low->in32.p, nullptr, low->out32.p, 1.0, 0.0, guard, &db, st)))
+        return rc;
+      GBPC_CUDA_TRY(launch_k(xpay_kernel<false, float>, vec_grid(n), kThreads, 0, st, n,
+                             (const KrylovScalars*)K(), (const float*)low->out32.as<float>(),
+                             p.as<double>(), (const double*)nullptr, (double*)nullptr));
+    } else if (method == GBPC_CG) {
+      DotSpec da = dot(p.as<double>(), FIN_CG_ALPHA);
+      if ((rc = A->apply(p.p, nullptr, Ap.p, 1.0, 0.0, guard, &da, st))) return rc;
+      GBPC_CUDA_TRY(launch_k(cg_update_kernel<false>, vec_grid(n), kThreads, 0, st, n, K(), x,
+                             r.as<double>(), (const double*)p.as<double>(),
+                             (const double*)Ap.as<double>(), (float*)nullptr, rrr));
       DotSpec db = dot(r.as<double>(), FIN_CG_BETA);
       if ((rc = precondition(r.as<double>(), z.as<double>(), guard, &db, st))) return rc;
       GBPC_CUDA_TRY(launch_k(xpay_kernel<false>, vec_grid(n), kThreads, 0, st, n,
@@ -434,6 +477,7 @@ extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_gr
   s.method = method;
   s.A = a;
   s.M = m;
+  s.low = dynamic_cast<LowPrecisionOp*>(m);
   s.n = a->rows;
   s.use_graph = use_graph != 0;
   if (unroll > 0) s.unroll = unroll > 64 ? 64 : unroll;

@@ -182,6 +182,41 @@ int scale_axpby(int vdtype, int64_t n, const void* d, const void* x, const void*
   return GBPC_OK;
 }
 
+// Float32 preconditioner behind a float64 interface (LowPrecisionOp).
+// out = (float) x, guarded like the products.
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
+narrow_kernel(int64_t n, const double* __restrict__ x, float* __restrict__ out, const int* guard) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (guard_off(guard)) return;
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kThreads)
+    out[i] = (float)x[i];
+}
+
+// z = alpha * (double) v + beta * y (beta == 0 never reads y), with the
+// fused dot(w, z) in float64.
+template <bool UNIT>
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
+widen_axpby_kernel(int64_t n, const float* __restrict__ v, const double* y, double* z,
+                   double alpha, double beta, int beta_zero, const int* guard, Reduction red) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (guard_off(guard)) return;
+  double part = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kThreads) {
+    double o = (double)v[i];
+    if (!UNIT) {
+      o = alpha * o;
+      if (!beta_zero) o = fma(beta, y[i], o);
+    }
+    z[i] = o;
+    if (red.w) part = fma(o, red.w[i], part);
+  }
+  if (red.w) reduce_and_finalize(red, part);
+}
+
 // ---------------------------------------------------------------------------
 // Operators.
 
@@ -312,6 +347,33 @@ struct Bilu0Op : Operator {
   bool gathers_x() const override { return false; }
 };
 
+}  // namespace
+
+int LowPrecisionOp::apply(const void* x, const void* y, void* z, double alpha, double beta,
+                          const int* guard, const DotSpec* dot, cudaStream_t st) {
+  // alpha == 0: z = beta * y without reading x (the operator contract).
+  if (alpha == 0.0) return scale_axpby(GBPC_F64, rows, nullptr, x, y, z, 0.0, beta, guard, dot, st);
+  const int g = elementwise_grid(rows);
+  // x is consumed into in32 before z is written, so x, y, z may alias.
+  GBPC_CUDA_TRY(launch_k(narrow_kernel, g, kThreads, 0, st, rows, (const double*)x,
+                         in32.as<float>(), guard));
+  int rc = inner->apply(in32.p, nullptr, out32.p, 1.0, 0.0, guard, nullptr, st);
+  if (rc) return rc;
+  const Reduction red = make_reduction(dot);
+  const bool unit = alpha == 1.0 && beta == 0.0;
+  if (unit)
+    GBPC_CUDA_TRY(launch_k(widen_axpby_kernel<true>, g, kThreads, 0, st, rows,
+                           (const float*)out32.as<float>(), (const double*)y, (double*)z, alpha,
+                           beta, 1, guard, red));
+  else
+    GBPC_CUDA_TRY(launch_k(widen_axpby_kernel<false>, g, kThreads, 0, st, rows,
+                           (const float*)out32.as<float>(), (const double*)y, (double*)z, alpha,
+                           beta, (int)(beta == 0.0), guard, red));
+  return GBPC_OK;
+}
+
+namespace {
+
 int check_dtypes(int value_dtype, int vector_dtype) {
   if (!valid_value_dtype(value_dtype)) {
     gbpc_set_error("value dtype must be float64, float32 or bfloat16");
@@ -388,9 +450,38 @@ extern "C" int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int
     gbpc_set_error("gbpc_op_fsai: bad arguments");
     return GBPC_ERR_ARG;
   }
-  int rc = check_dtypes(value_dtype, vector_dtype);
+  const bool low = vector_dtype == GBPC_F32_APPLY;
+  if (low && value_dtype != GBPC_F32 && value_dtype != GBPC_BF16) {
+    gbpc_set_error("float32 application needs float32 or bfloat16 factor storage");
+    return GBPC_ERR_ARG;
+  }
+  int rc = check_dtypes(value_dtype, low ? GBPC_F32 : vector_dtype);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  if (low) {
+    // The float32 operator, wrapped behind float64 vectors.
+    gbpc_op* inner = nullptr;
+    rc = gbpc_op_fsai(nrow, block, g_off, g_col, g_val, gt_off, gt_col, gt_val, value_dtype,
+                      GBPC_F32, stream, &inner);
+    if (rc) return rc;
+    auto* w = new LowPrecisionOp;
+    w->inner = std::move(inner->impl);
+    delete inner;
+    w->device_bytes = w->inner->device_bytes;
+    {
+      ByteTally tally(&w->device_bytes);
+      w->rows = (int64_t)nrow * block;
+      w->vdtype = GBPC_F64;
+      rc = w->in32.alloc(sizeof(float) * std::max<int64_t>(w->rows, 1));
+      if (!rc) rc = w->out32.alloc(sizeof(float) * std::max<int64_t>(w->rows, 1));
+    }
+    if (rc) {
+      delete w;
+      return rc;
+    }
+    GBPC_OUT_OP(w);
+    return GBPC_OK;
+  }
   auto* op = new FsaiOp;
   ByteTally tally(&op->device_bytes);
   op->rows = (int64_t)nrow * block;
@@ -420,7 +511,9 @@ extern "C" int gbpc_op_fsai_refill(gbpc_op* h, const int32_t* g_off, const int32
                                    const void* g_val, const int32_t* gt_off,
                                    const int32_t* gt_col, const void* gt_val, int value_dtype,
                                    void* stream) {
-  auto* op = h ? dynamic_cast<FsaiOp*>(h->impl.get()) : nullptr;
+  Operator* base = h ? h->impl.get() : nullptr;
+  if (auto* low = dynamic_cast<LowPrecisionOp*>(base)) base = low->inner.get();
+  auto* op = dynamic_cast<FsaiOp*>(base);
   if (!op || !g_off || !gt_off || !valid_value_dtype(value_dtype)) {
     gbpc_set_error("gbpc_op_fsai_refill: needs an FSAI operator and its factor arrays");
     return GBPC_ERR_ARG;

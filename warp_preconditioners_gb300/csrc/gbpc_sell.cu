@@ -491,10 +491,9 @@ int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, 
               cudaStream_t st) {
   Reduction red{};
   if (dot != nullptr && dot->w != nullptr) {
-    if (adtype != GBPC_F64) {
-      gbpc_set_error("fused dot products need float64 vectors");
-      return GBPC_ERR_ARG;
-    }
+    // The weight is float64 whatever the product's vectors; a float32
+    // output is widened before it is multiplied (the float32-applied
+    // preconditioner inside the float64 CG loop).
     red.w = dot->w;
     red.partials = dot->rb->partials.as<double>();
     red.counter = dot->rb->counter.as<unsigned int>();

@@ -76,10 +76,20 @@ class FSAI(LinearOperator):
     Setup synchronises; apply is stream-ordered and graph-capturable.  With
     ``reuse_pattern=True``, ``update(A)`` refits the original supports for new
     values on the same topology (fsai_reuse.py).
+
+    ``apply_dtype=torch.float32`` (an addition of this build; float64
+    matrices only) applies the factor with float32 arithmetic behind the
+    float64 vector interface: G stored in float32 (or bfloat16 with
+    ``factor_dtype=torch.bfloat16``), the input narrowed, products summed in
+    float32, the result widened.  Inside ``linear.cg`` / ``Solver`` the
+    conversions are fused into the loop's own vector kernels, so the
+    preconditioner streams half (bfloat16: three eighths) of the float64
+    factor's bytes and issues no float64 arithmetic, while the Krylov
+    recurrences, dot products and the system operator stay float64.
     """
 
     def __init__(self, A, max_row_size=8, kap_tolerance=1.0e-3, pivot_floor=None, apply_lanes=1,
-                 factor_dtype=None, reuse_pattern=False, max_step_size=1):
+                 factor_dtype=None, reuse_pattern=False, max_step_size=1, apply_dtype=None):
         if (not isinstance(A, BsrMatrix) or A.shape[0] != A.shape[1]
                 or A.block_shape[0] != A.block_shape[1]):
             raise ValueError("FSAI requires a square BSR matrix with square blocks")
@@ -99,8 +109,13 @@ class FSAI(LinearOperator):
             raise ValueError("pivot_floor must be in (0, 1)")
         if not isinstance(apply_lanes, int) or apply_lanes not in (1, 2, 4, 8, 16, 32):
             raise ValueError("apply_lanes must be one of 1, 2, 4, 8, 16, 32")
+        if apply_dtype not in (None, A.scalar_type, torch.float32):
+            raise ValueError("apply_dtype must be the matrix scalar type or torch.float32")
+        low = apply_dtype == torch.float32 and A.scalar_type == torch.float64
         if factor_dtype is None:
-            factor_dtype = A.scalar_type
+            factor_dtype = torch.float32 if low else A.scalar_type
+        if low and factor_dtype not in (torch.float32, torch.bfloat16):
+            raise ValueError("apply_dtype=torch.float32 needs float32 or bfloat16 factor storage")
         if factor_dtype != A.scalar_type and not (
             A.scalar_type == torch.float64 and factor_dtype in (torch.float32, torch.bfloat16)
         ):
@@ -131,8 +146,9 @@ class FSAI(LinearOperator):
         self._op = _lib.new_op(
             "gbpc_op_fsai", n, 1, _lib.ptr(self.G.offsets), _lib.ptr(self.G.columns),
             _lib.ptr(self.G.values), _lib.ptr(self.GT.offsets), _lib.ptr(self.GT.columns),
-            _lib.ptr(self.GT.values), _lib.dtype_code(factor_dtype), _lib.dtype_code(dt),
-            _lib.stream(A.device))
+            _lib.ptr(self.GT.values), _lib.dtype_code(factor_dtype),
+            _lib.GBPC_F32_APPLY if low else _lib.dtype_code(dt), _lib.stream(A.device))
+        self.apply_dtype = torch.float32 if low else dt
         super().__init__(A.shape, dt, A.device, self._apply)
         self._refit = _RefitPlan(self, A, max_row_size, pivot_floor) if reuse_pattern else None
 
