@@ -415,8 +415,11 @@ def main():
     peak = float(peaks["hbm_gbs"])
     achieved = it_bytes * total_iters / solve_total_s / 1e9
 
-    apply = measure_applies(pre, K, mass, free, n, dev)
+    apply = measure_applies(
+        pre, lambda: FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
+                          kap_tolerance=1e-3), K, mass, free, n, dev)
     traffic = read_traffic()
+    fp64_peak = measure_fp64_peak(dev)
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
@@ -441,7 +444,8 @@ def main():
             "traffic": traffic,
         },
         "roofline_fp64": pcg_fp64_roofline(n, prob["K"].nnz, nnz_g, nnz_gt, total_iters,
-                                           solve_total_s),
+                                           solve_total_s, fp64_peak),
+        "fp64_peak": fp64_peak,
         "apply_gbps": apply,
         "gpu_launches": launch_count(iters),
     }
@@ -472,7 +476,7 @@ def main():
             "sampled_fraction": min(1.0, cb["iters_sampled"] / float(sum(iters[-1]))),
         }
         line["fsai_setup_roofline"] = fsai_setup_roofline(cb["setup_flops"],
-                                                          line["refit"]["setup_ms"])
+                                                          line["refit"]["setup_ms"], fp64_peak)
         line["parity"] = factor_parity(pre, *cb["factor"])
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -480,29 +484,67 @@ def main():
         dist.destroy_process_group()
 
 
-FP64_PEAK_TFLOPS = 1.25  # GB300 nominal FP64; not among the measured peaks
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal FP64, used only when the probe fails
 
 
-def pcg_fp64_roofline(n, nnz_k, nnz_g, nnz_gt, total_iters, solve_s):
+def measure_fp64_peak(dev, iters=20000):
+    """FP64 FMA throughput of this GPU, measured live: libgbpc's
+    gbpc_fma_probe (8 independent FMA chains per thread, 8 CTAs of 256
+    threads per SM) timed with CUDA events on the launching stream, best of
+    3 after a warm-up.  TFLOP/s counts a multiply-add as 2 flops."""
+    import ctypes
+
+    import torch
+
+    from warp_preconditioners_gb300 import _lib
+
+    ctas = 152 * 8
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    st = _lib.stream(dev)
+    stream = torch.cuda.current_stream(dev)
+    _lib.call("gbpc_fma_probe", 100, ctas, _lib.ptr(out), st)
+    best = None
+    for _ in range(3):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        _lib.call("gbpc_fma_probe", ctypes.c_int64(iters), ctas, _lib.ptr(out), st)
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        t = s.elapsed_time(e) / 1e3
+        best = t if best is None else min(best, t)
+    fmas = ctas * 256 * 8 * iters
+    return {"tflops": 2 * fmas / best / 1e12, "fma_per_s": fmas / best, "ms": best * 1e3,
+            "how": f"gbpc_fma_probe: {ctas} CTAs x 256 threads x 8 chains x {iters} FMAs, "
+                   "CUDA events, best of 3"}
+
+
+def _fp64_peak(peak):
+    if peak:
+        return peak["tflops"], "measured in this run (gbpc_fma_probe, FP64 FMA chains)"
+    return FP64_NOMINAL_TFLOPS, "GB300 nominal FP64 (fallback: the probe did not run)"
+
+
+def pcg_fp64_roofline(n, nnz_k, nnz_g, nnz_gt, total_iters, solve_s, peak=None):
     """The same timed iterations against FP64 arithmetic (a multiply-add is 2
     flops): 2 per stored entry of the two K products, of G and of G^T, and
     15 n for the epilogues, the x/r/p updates and the three dot products."""
     flops = 2 * (2 * nnz_k + nnz_g + nnz_gt) + 15 * n
     achieved = flops * total_iters / solve_s / 1e12
+    p, src = _fp64_peak(peak)
     return {"bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops_per_iteration": flops,
-            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "frac": achieved / FP64_PEAK_TFLOPS,
-            "peak_source": "GB300 nominal FP64 (fallback: no FP64 figure in MEASURED_PEAKS.json)"}
+            "achieved": achieved, "peak": p, "frac": achieved / p, "peak_source": src}
 
 
-def fsai_setup_roofline(flops, setup_ms):
+def fsai_setup_roofline(flops, setup_ms, peak=None):
     """FP64 roofline of the FSAI setup: the oracle's exact operation count of
     the same setup (each separately rounded multiply, add, divide, square
     root; the reference evaluates without contraction) over the GPU
     constructor's CUDA-event time (build, pack, transpose, operator copies)."""
     achieved = flops / (setup_ms * 1e-3) / 1e12
+    p, src = _fp64_peak(peak)
     return {"bound": "fp64", "unit": "TFLOP/s", "flops": flops, "setup_ms": setup_ms,
-            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "frac": achieved / FP64_PEAK_TFLOPS,
-            "peak_source": "GB300 nominal FP64 (fallback: no FP64 figure in MEASURED_PEAKS.json)"}
+            "achieved": achieved, "peak": p, "frac": achieved / p, "peak_source": src}
 
 
 def replica_aggregate(elapsed_ms, local_solves, dist, device):
@@ -554,8 +596,9 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
         return X, nit.clone()
 
     def batch_f32m(factor_dtype):
+        # The batched operator narrows the float32 factor to factor_dtype itself.
         pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3,
-                   apply_dtype=torch.float32, factor_dtype=factor_dtype)
+                   factor_dtype=torch.float32)
         bs = batched.BatchedSolver(K, mass, ALPHA, pre, factor_dtype=factor_dtype,
                                    apply_dtype=torch.float32)
         X = torch.zeros_like(B)
@@ -633,10 +676,10 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
     return out
 
 
-def measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev, ms_per_step):
+def _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step, pre_kw, solver_kw):
     """The default step (setup + 4 sequential CG solves through linear.Solver)
-    with the FSAI factor applied in float32 (stored in bfloat16 or float32),
-    everything else float64; CUDA-event medians of 3 steps."""
+    with extra FSAI / Solver keyword arguments; CUDA-event median of 3 steps,
+    iteration counts and per-RHS backward error against the assembled Q."""
     import torch
 
     from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, linear
@@ -644,44 +687,51 @@ def measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev, ms_per_step):
     n = prob["n"]
     rhs = torch.as_tensor(prob["rhs"], device=dev).contiguous()
     b = torch.empty(n, dtype=torch.float64, device=dev)
+    xs = torch.zeros((4, n), dtype=torch.float64, device=dev)
+
+    def step():
+        op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
+        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
+                   kap_tolerance=1e-3, **pre_kw)
+        solver = linear.Solver(args.method, op, pre, **solver_kw)
+        its = []
+        for j in range(4):
+            b.copy_(rhs[j])
+            xs[j].zero_()
+            nit, _, _ = solver.run(b, xs[j], tol=args.rtol, maxiter=100000)
+            its.append(nit.clone())
+        return its
+
+    step()
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        its = step()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    t = statistics.median(times)
+    qh = prob["Q"]
+    sols = xs.cpu().numpy()
+    absq = abs(qh)
+    berr = [float(np.max(np.abs(prob["rhs"][j] - qh @ sols[j])
+                         / (absq @ np.abs(sols[j]) + np.abs(prob["rhs"][j]))))
+            for j in range(4)]
+    return {"ms_per_step": t, "solves_per_s": 4e3 / t, "speedup_vs_drop_in": ms_per_step / t,
+            "iterations": [int(i.item()) for i in its], "backward_error_max": max(berr)}
+
+
+def measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev, ms_per_step):
+    """The default step with the FSAI factor applied in float32 (stored in
+    bfloat16 or float32), everything else float64."""
+    import torch
+
     out = {}
-    for dt in (torch.bfloat16, torch.float32):
-        xs = torch.zeros((4, n), dtype=torch.float64, device=dev)
-
-        def step():
-            op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
-            pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
-                       kap_tolerance=1e-3, apply_dtype=torch.float32, factor_dtype=dt)
-            solver = linear.Solver(args.method, op, pre)
-            its = []
-            for j in range(4):
-                b.copy_(rhs[j])
-                xs[j].zero_()
-                nit, _, _ = solver.run(b, xs[j], tol=args.rtol, maxiter=100000)
-                its.append(nit.clone())
-            return its
-
-        step()
-        times = []
-        for _ in range(3):
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            its = step()
-            e1.record()
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1))
-        t = statistics.median(times)
-        qh = prob["Q"]
-        sols = xs.cpu().numpy()
-        absq = abs(qh)
-        berr = [float(np.max(np.abs(prob["rhs"][j] - qh @ sols[j])
-                             / (absq @ np.abs(sols[j]) + np.abs(prob["rhs"][j]))))
-                for j in range(4)]
-        name = "bf16" if dt == torch.bfloat16 else "f32"
-        out[name] = {"ms_per_step": t, "solves_per_s": 4e3 / t,
-                     "speedup_vs_drop_in": ms_per_step / t,
-                     "iterations": [int(i.item()) for i in its], "backward_error_max": max(berr)}
+    for name, dt in (("bf16", torch.bfloat16), ("f32", torch.float32)):
+        out[name] = _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step,
+                                  dict(apply_dtype=torch.float32, factor_dtype=dt), {})
     out["solver"] = ("the default step (setup + 4 sequential CG solves) with FSAI(..., "
                      "apply_dtype=torch.float32): factor stored in bf16 / f32 and applied in "
                      "float32; operator, recurrences and dots float64")
@@ -1123,10 +1173,13 @@ def run_c5(args, dev):
     # (|A| |x| >> |b|); the second is the accuracy measure.
     acc = {kind: {"rel": [], "berr": []} for kind in serve.KINDS}
     nonfinite = 0
+    assembled = {}
     for req, r in zip(stream, served):
         if r.ok and r.x is not None:
             h = cat.get(req.key)
-            A = h.A if h.kind == "laplacian" else h.P
+            if req.key not in assembled:  # host assembly for the check only
+                assembled[req.key] = h.assembled()
+            A = assembled[req.key]
             b, x = serve.request_rhs(req).numpy(), r.x.numpy()
             if not np.isfinite(x).all():
                 nonfinite += 1
@@ -1177,48 +1230,72 @@ def launch_count(iters):
     return sum(setup + sum(7 + 6 * i for i in step) for step in iters)
 
 
-def measure_applies(pre, K, mass, free, n, dev):
-    """Live CUDA-event timing of the two applies on the step's data: 50
-    back-to-back applies replayed from one graph, algorithmic bytes over the
-    time (GB/s).  The FSAI factor (66 MB) stays in L2 between them, so this
-    is the apply's FP64-bound rate, not an HBM figure (the PCG roofline is
-    the HBM one)."""
+def _graph_time(fns, reps, dev):
+    """Seconds per call of the calls in `fns` (cycled), `reps` of them
+    replayed from one CUDA graph, CUDA events around a warm replay."""
+    import torch
+
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for fn in fns:
+            fn()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        for r in range(reps):
+            fns[r % len(fns)]()
+    graph.replay()
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    graph.replay()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps / 1e3
+
+
+def measure_applies(pre, make_pre, K, mass, free, n, dev, copies=5):
+    """Live CUDA-event timing of the two applies on the step's data,
+    algorithmic bytes over the time (GB/s), two ways:
+
+    * ``resident``: 50 back-to-back applies of one operator replayed from one
+      graph; the FSAI factor (66 MB) stays in L2 between them, so this is the
+      apply's issue-bound rate, not an HBM figure;
+    * ``hbm``: 50 applies cycling over `copies` independent operators and
+      vectors (more than twice the 129 MB L2 in total), so every apply reads
+      its matrices from HBM.  Reuse inside one apply (the factored operator
+      reads its one copy of L twice) still counts, as it does in a solve.
+    """
     import torch
 
     from warp_preconditioners_gb300 import SquaredLaplacianOperator
 
-    op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
-    x = torch.randn(n, dtype=torch.float64, device=dev)
-    z = torch.empty_like(x)
+    ops = [SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA) for _ in range(copies)]
+    pres = [pre] + [make_pre() for _ in range(copies - 1)]
+    xs = [torch.randn(n, dtype=torch.float64, device=dev) for _ in range(copies)]
+    zs = [torch.empty_like(x) for x in xs]
     out = {}
     reps = 50
-    for name, fn, nbytes in (
-        ("fsai_apply", lambda: pre.matvec(x, x, z, 1.0, 0.0),
-         (pre.G.nnz + pre.GT.nnz) * 12 + 2 * 4 * (n + 1) + 4 * n * 8),
-        ("factored_operator_apply", lambda: op.matvec(x, x, z, 1.0, 0.0),
-         2 * (K.nnz * 12 + 4 * (n + 1)) + 6 * n * 8),
+    fsai_bytes = (pre.G.nnz + pre.GT.nnz) * 12 + 2 * 4 * (n + 1) + 4 * n * 8
+    op_bytes = 2 * (K.nnz * 12 + 4 * (n + 1)) + 6 * n * 8
+
+    def fsai_call(c):
+        return lambda: pres[c].matvec(xs[c], xs[c], zs[c], 1.0, 0.0)
+
+    def op_call(c):
+        return lambda: ops[c].matvec(xs[c], xs[c], zs[c], 1.0, 0.0)
+
+    for name, make, nbytes, footprint in (
+        ("fsai_apply", fsai_call, fsai_bytes, fsai_bytes),
+        ("factored_operator_apply", op_call, op_bytes, K.nnz * 12 + 6 * n * 8),
     ):
-        # Replay `reps` applies from one CUDA graph so the host launch path is
-        # not what gets timed.
-        side = torch.cuda.Stream(dev)
-        side.wait_stream(torch.cuda.current_stream(dev))
-        with torch.cuda.stream(side):
-            fn()
-        torch.cuda.current_stream(dev).wait_stream(side)
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph):
-            for _ in range(reps):
-                fn()
-        graph.replay()
-        torch.cuda.synchronize()
-        s = torch.cuda.Event(enable_timing=True)
-        e = torch.cuda.Event(enable_timing=True)
-        s.record()
-        graph.replay()
-        e.record()
-        torch.cuda.synchronize()
-        t = s.elapsed_time(e) / reps / 1e3
-        out[name] = {"us": t * 1e6, "gbps": nbytes / t / 1e9, "bytes": nbytes}
+        t_res = _graph_time([make(0)], reps, dev)
+        t_hbm = _graph_time([make(c) for c in range(copies)], reps, dev)
+        out[name] = {"us": t_res * 1e6, "gbps": nbytes / t_res / 1e9, "bytes": nbytes,
+                     "hbm": {"us": t_hbm * 1e6, "gbps": nbytes / t_hbm / 1e9,
+                             "copies": copies, "rotated_bytes": copies * footprint}}
     return out
 
 

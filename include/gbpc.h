@@ -432,6 +432,55 @@ int gbpc_refine(gbpc_bop* A64, gbpc_bsolver* inner, int k, const double* B, doub
                 double tol_outer, double tol_inner, int max_outer, int max_inner,
                 int32_t* outer_host, int32_t* inner_host, void* stream);
 
+/* Many independent systems of uneven size in one solve: preconditioned CG
+ * on a block-diagonal A (and M) whose diagonal blocks are the systems,
+ * system s owning rows [seg_rows_host[s], seg_rows_host[s + 1]).  Each
+ * product is one launch for all systems; alpha, beta, the dot products,
+ * the stopping test (r_s.r_s <= max(atol, tol |b_s|)^2 or maxiter, maxiter
+ * <= 0 meaning the system's size) and the iteration count are per system,
+ * and a system's iterates do not depend on the others in the solve.  Whole
+ * loop in one CUDA graph (use_graph != 0) or a host loop of the same
+ * kernels.  nit_dev / rr_dev / atol_sq_dev: nseg entries each (any may be
+ * NULL).  No reference counterpart (the reference solves one system per
+ * warp.optim.linear.cg call, benchmarks/block_challenge.py:131-139). */
+typedef struct gbpc_msolver gbpc_msolver;
+int gbpc_msolver_create(gbpc_op* A, gbpc_op* M, int nseg, const int64_t* seg_rows_host,
+                        int use_graph, int unroll, void* stream, gbpc_msolver** out);
+int gbpc_msolver_run(gbpc_msolver* solver, const double* b, double* x, double tol, double atol,
+                     int maxiter, int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
+                     void* stream);
+int gbpc_msolver_device_bytes(const gbpc_msolver* solver, size_t* bytes_host);
+int gbpc_msolver_destroy(gbpc_msolver* solver);
+
+/* ------------------------------------------------------------------------ */
+/* Vector utilities (dtype GBPC_F64 or GBPC_F32; stream-ordered, no
+ * allocation, no synchronisation).                                          */
+/* ------------------------------------------------------------------------ */
+
+/* out[i] = 2 randi(rand_init(seed, i), 0, 2) - 1: the seeded Rademacher probe
+ * of FSAI.quality (warp_preconditioners/fsai_reuse.py:143-147, the `probe`
+ * kernel), drawn from Warp's PCG-hash stream. */
+int gbpc_rademacher(int64_t n, int seed, int dtype, void* out, void* stream);
+
+/* z = alpha x + beta y (alpha == 0 never reads x, beta == 0 never reads y;
+ * z may alias x or y).  The vector update warp.optim.linear's loops and
+ * fsai_reuse.py:149-152 (`subtract`) perform with Warp array ops. */
+int gbpc_vec_axpby(int64_t n, int dtype, double alpha, const void* x, double beta,
+                   const void* y, void* z, void* stream);
+
+/* *result (device float64) = x . y accumulated in float64 in a fixed order
+ * (the same value on every run), replacing warp.utils.array_inner
+ * (fsai_reuse.py:277).  `work`: gbpc_vec_dot_work_size() device doubles. */
+int gbpc_vec_dot_work_size(void);
+int gbpc_vec_dot(int64_t n, int dtype, const void* x, const void* y, double* work,
+                 double* result, void* stream);
+
+/* FP64 FMA throughput probe: `ctas` CTAs of 256 threads, each thread 8
+ * independent FMA chains of `iters` steps (8 * iters FMAs).  `out` holds 2
+ * device doubles.  No reference counterpart: the benchmark times it to
+ * measure the FP64 peak it divides by. */
+int gbpc_fma_probe(int64_t iters, int ctas, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -276,6 +276,46 @@ def fsai_apply(g: CSR, gt: CSR, x, y, alpha, beta, accum_dtype=np.float64):
     return csr_spmv(gt, tmp, y, alpha, beta, accum_dtype)
 
 
+def _pcg_hash(v):
+    """The PCG hash (Jarzynski and Olano, JCGT 9(3), 2020) on uint32 arrays."""
+    v = np.asarray(v, np.uint32)
+    with np.errstate(over="ignore"):
+        state = v * np.uint32(747796405) + np.uint32(2891336453)
+        word = ((state >> ((state >> np.uint32(28)) + np.uint32(4))) ^ state) * np.uint32(277803737)
+    return (word >> np.uint32(22)) ^ word
+
+
+def rademacher(n, seed, dtype=np.float64):
+    """Probe of FSAI.quality, warp_preconditioners/fsai_reuse.py:143-147:
+    out[i] = 2 randi(rand_init(seed, i), 0, 2) - 1, with Warp's
+    rand_init(seed, i) = pcg(seed + pcg(i)) and randi advancing the state by
+    one hash and returning lo + state % (hi - lo)."""
+    i = np.arange(n, dtype=np.uint32)
+    with np.errstate(over="ignore"):
+        state = _pcg_hash(np.uint32(seed & 0xFFFFFFFF) + _pcg_hash(i))
+    draw = _pcg_hash(state)
+    return (2 * (draw % np.uint32(2)).astype(np.int64) - 1).astype(dtype)
+
+
+def fsai_quality(a: CSR, g: CSR, gt: CSR, probes=4, seed=17):
+    """||G A G^T - I||_F / sqrt(n) estimated with the reference's probes
+    (warp_preconditioners/fsai_reuse.py:248-279): per probe x,
+    w = G (A (G^T x)) - x and total += w.w; result sqrt(total / (probes n))."""
+    n = a.nrow
+    if n == 0:
+        return 0.0
+    dt = a.values.dtype
+    zero = np.zeros(n, dt)
+    total = 0.0
+    for p in range(probes):
+        x = rademacher(n, seed + p, dt)
+        y = csr_spmv(gt, x, zero, 1.0, 0.0, dt)
+        z = csr_spmv(a, y, zero, 1.0, 0.0, dt)
+        w = csr_spmv(g, z, zero, 1.0, 0.0, dt) - x
+        total += float(np.dot(w.astype(np.float64), w.astype(np.float64)))
+    return (total / (probes * n)) ** 0.5
+
+
 def bsr_spmv(nrow, b, offsets, columns, values, x, y, alpha, beta):
     values = np.ascontiguousarray(values)
     x = np.ascontiguousarray(x, np.float64).reshape(-1)

@@ -21,6 +21,9 @@ preconditioners on seeded inputs and stores inputs and outputs in
   and one 3-sweep apply, the scalarised FSAI (width 8, kap 3e-3, float32
   factor), and the block FSAI candidate's scalar factor for 2 and 4 blocks
   (benchmarks/block_fsai_candidate.py).
+* ``ref_quality.npz``: ``FSAI.quality`` values (4 probes seed 17, 2 probes
+  seed 5) on the 6^3 tet-cube Q and the 32 x 32 Laplacian with their
+  factors, and the reference's Rademacher probe vectors for four seeds.
 * ``ref_ops.npz``: products of the factored squared-Laplacian operator
   (warp_preconditioners/squared_laplacian.py) on the 8^3 tet cube with its
   boundary vertices constrained: an apply with aliasing-free x, y and the
@@ -185,8 +188,37 @@ def operator_cases():
     print("operator cases done", flush=True)
 
 
+def quality_cases():
+    """FSAI.quality (warp_preconditioners/fsai_reuse.py:248-279) on the 6^3
+    tet-cube Q (w8 factor) and the 32 x 32 Laplacian (w4 factor), with the
+    reference's own probe vectors (its `probe` kernel, fsai_reuse.py:143-147)."""
+    from warp_preconditioners.fsai_reuse import kernels
+
+    out = {}
+    verts, tets, K, mass = problems.tet_cube(6)
+    Q = problems.biharmonic(K, mass, ALPHA)
+    lap = problems.laplacian_2d(32)
+    for tag, a, width in (("cube6", Q, 8), ("lap32", lap, 4)):
+        put_csr(out, tag + "_A", a.indptr, a.indices, a.data)
+        pre = FSAI(from_scipy(a), max_row_size=width)
+        put_bsr(out, tag + "_G", pre.G)
+        put_bsr(out, tag + "_GT", pre.GT)
+        for probes, seed in ((4, 17), (2, 5)):
+            out[f"{tag}_quality_p{probes}_s{seed}"] = np.float64(pre.quality(probes=probes,
+                                                                             seed=seed))
+    probe = kernels(wp.float64, wp.float64, 8)[3]
+    for seed in (17, 18, 5, 123456):
+        x = wp.empty(300, dtype=wp.float64)
+        wp.launch(probe, 300, [seed, x])
+        out[f"probe_s{seed}"] = x.numpy().copy()
+    np.savez_compressed(HERE / "ref_quality.npz", **out)
+    print("quality cases done", flush=True)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["fsai", "block", "ops"]
+    which = sys.argv[1:] or ["fsai", "block", "ops", "quality"]
+    if "quality" in which:
+        quality_cases()
     if "block" in which:
         block_cases()
     if "ops" in which:

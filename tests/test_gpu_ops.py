@@ -147,6 +147,43 @@ def test_tet_cube_factored_equals_assembled(oracle):
     np.testing.assert_allclose(z1.cpu().numpy(), ref, rtol=1e-12, atol=1e-15)
 
 
+def test_identity_free_shares_one_copy_of_L(oracle):
+    # With every vertex free in index order one stored copy of L serves the
+    # forward and backward products, the forward one walking its slices in
+    # reverse.  At 56^3 (5,488 slices) the walk has a partial last pass.
+    # The same system with its unknowns listed in a random order takes the
+    # two-copy path; both must give the oracle's product, and the two paths
+    # the same vector up to the reordering.
+    from warp_preconditioners_gb300 import SquaredLaplacianOperator, from_scipy, problems
+
+    _, _, K, mass = problems.tet_cube(56)
+    n = K.shape[0]
+    dev = cuda()
+    Kd, md = from_scipy(K, dev), vec(mass)
+    rng = np.random.default_rng(5)
+    x_np = rng.normal(size=n)
+    perm = rng.permutation(n).astype(np.int32)
+    ident = SquaredLaplacianOperator(Kd, md, torch.arange(n, dtype=torch.int32, device=dev),
+                                     mass_weight=1e-4)
+    permuted = SquaredLaplacianOperator(Kd, md, torch.as_tensor(perm, device=dev),
+                                        mass_weight=1e-4)
+    x = vec(x_np)
+    z1 = torch.empty_like(x)
+    ident.matvec(x, x, z1, 1.0, 0.0)
+    z1b = torch.empty_like(x)
+    ident.matvec(x, x, z1b, 1.0, 0.0)
+    assert torch.equal(z1, z1b)
+    xp = vec(x_np[perm])
+    z2 = torch.empty_like(xp)
+    permuted.matvec(xp, xp, z2, 1.0, 0.0)
+    ref = oracle.Operator.sqlap(oracle_csr(oracle, K), mass, 1e-4).apply(x_np, np.zeros(n),
+                                                                         1.0, 0.0)
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(z1.cpu().numpy(), ref, rtol=1e-12, atol=1e-14 * scale)
+    np.testing.assert_allclose(z2.cpu().numpy(), z1.cpu().numpy()[perm], rtol=1e-12,
+                               atol=1e-14 * scale)
+
+
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 @pytest.mark.parametrize("size", [1, 2, 3, 4])
 def test_block_factors_and_aliases(oracle, dtype, size):

@@ -150,3 +150,22 @@ def test_factored_operator_and_fsai_apply(ref_ops, ref_fsai):
     zq = torch.empty(len(ref_ops["cube8_xq"]), dtype=torch.float64, device=cuda())
     pre.matvec(vec(ref_ops["cube8_xq"]), vec(ref_ops["cube8_yq"]), zq, 0.7, -0.2)
     _close(zq.cpu().numpy(), ref_ops["cube8_fsai_apply"])
+
+
+def test_quality_probes_and_value():
+    # FSAI.quality against the reference's value (fsai_reuse.py:248-279) and
+    # the device Rademacher probes against its probe kernel, bit for bit.
+    from warp_preconditioners_gb300 import FSAI, _lib
+
+    f = np.load(GOLDEN / "ref_quality.npz")
+    x = torch.empty(300, dtype=torch.float64, device=cuda())
+    for seed in (17, 18, 5, 123456):
+        _lib.call("gbpc_rademacher", 300, seed, _lib.GBPC_F64, _lib.ptr(x), _lib.stream(cuda()))
+        np.testing.assert_array_equal(x.cpu().numpy(), f[f"probe_s{seed}"])
+    for tag, width in (("cube6", 8), ("lap32", 4)):
+        pre = FSAI(_matrix(f, tag + "_A"), max_row_size=width)
+        assert_factor_equal(pre.G, f, tag + "_G")
+        for probes, seed in ((4, 17), (2, 5)):
+            want = float(f[f"{tag}_quality_p{probes}_s{seed}"])
+            got = pre.quality(probes=probes, seed=seed)
+            assert abs(got - want) <= 1e-12 * want, (tag, probes, seed, got, want)

@@ -54,6 +54,25 @@ def ref_ops():
     return np.load(GOLDEN / "ref_ops.npz")
 
 
+@pytest.fixture(scope="module")
+def ref_quality():
+    return np.load(GOLDEN / "ref_quality.npz")
+
+
+def test_quality_probes_and_value(oracle, ref_quality):
+    # The reference's own probe kernel output, bit for bit, and its quality
+    # value to rounding (the dots are summed in a different order).
+    for seed in (17, 18, 5, 123456):
+        np.testing.assert_array_equal(oracle.rademacher(300, seed), ref_quality[f"probe_s{seed}"])
+    for tag in ("cube6", "lap32"):
+        a = _csr(oracle, ref_quality, tag + "_A")
+        g, gt = _csr(oracle, ref_quality, tag + "_G"), _csr(oracle, ref_quality, tag + "_GT")
+        for probes, seed in ((4, 17), (2, 5)):
+            want = float(ref_quality[f"{tag}_quality_p{probes}_s{seed}"])
+            got = oracle.fsai_quality(a, g, gt, probes, seed)
+            assert abs(got - want) <= 1e-12 * want, (tag, got, want)
+
+
 def test_fsai_laplacian64(oracle, ref_fsai):
     g, gt, _ = oracle.fsai(_csr(oracle, ref_fsai, "lap64_A"), width=8, step=1, tol=1e-3)
     assert_csr_equal(g, ref_fsai, "lap64_w8s1_G")

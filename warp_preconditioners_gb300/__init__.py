@@ -13,7 +13,7 @@ plus ``linear.cg`` / ``linear.cr`` / ``linear.gmres`` / ``linear.preconditioner`
 Vectors and matrices are torch CUDA tensors.
 """
 
-from . import batched, linear, sparse
+from . import batched, linear, multi, sparse
 from .biharmonic import BiharmonicSystem, RepeatedFSAI
 from .block_fsai import BlockFSAI, BsrBlockFSAI
 from .block_ilu import BlockILU0, BlockJacobi
@@ -49,6 +49,7 @@ __all__ = [
     "from_scipy",
     "batched",
     "linear",
+    "multi",
     "preconditioner",
     "sparse",
 ]

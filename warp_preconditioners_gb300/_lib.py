@@ -106,6 +106,15 @@ _SIGNATURES = {
     "gbpc_bsolver_device_bytes": [_vp, _szp],
     "gbpc_bsolver_destroy": [_vp],
     "gbpc_refine": [_vp, _vp, _int, _vp, _vp, _dbl, _dbl, _int, _int, _i32p, _i32p, _vp],
+    "gbpc_rademacher": [ctypes.c_int64, _int, _int, _vp, _vp],
+    "gbpc_vec_axpby": [ctypes.c_int64, _int, _dbl, _vp, _dbl, _vp, _vp, _vp],
+    "gbpc_vec_dot_work_size": [],
+    "gbpc_vec_dot": [ctypes.c_int64, _int, _vp, _vp, _vp, _vp, _vp],
+    "gbpc_fma_probe": [ctypes.c_int64, _int, _vp, _vp],
+    "gbpc_msolver_create": [_vp, _vp, _int, _i64p, _int, _int, _vp, ctypes.POINTER(_vp)],
+    "gbpc_msolver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
+    "gbpc_msolver_device_bytes": [_vp, _szp],
+    "gbpc_msolver_destroy": [_vp],
 }
 
 _lock = threading.Lock()

@@ -68,6 +68,8 @@ struct SellView {
   const V* vals;
   const int32_t* perm;  // stored row k is matrix row perm[k] (nullptr: identity)
   const int4* sched;    // SliceTask[nslices], slices by width descending
+  int reverse;          // walk each warp's passes last to first (see warp_slice)
+  int* err;             // set to 1 by a kernel whose bounded wait gave up (nullable)
 };
 
 // One entry of a sliced-ELL product schedule: slice s, its width (entries
@@ -89,6 +91,26 @@ __device__ __forceinline__ SliceTask load_task(const int4* sched, int64_t idx) {
 // one of the widest slices of a pass takes one of the narrowest of the next.
 __device__ __forceinline__ int64_t sched_index(int i, int t, int warps_total) {
   return (int64_t)i * warps_total + ((i & 1) ? warps_total - 1 - t : t);
+}
+
+// Schedule position of warp t's k-th slice (k = 0, 1, ...), or -1 when it
+// has no k-th slice.  Forward: passes 0, 1, ...  Reverse: the same passes
+// last to first (a partial last pass that misses warp t is skipped), so a
+// product that follows another over the same matrix starts with the slices
+// that product touched last, which are the ones most likely still in L2.
+// Each warp takes the same set of slices either way; only a fused dot
+// product's summation order would change, so reverse walks are used for
+// products without one.
+__device__ __forceinline__ int64_t warp_slice(int k, int t, int warps_total, int64_t nslices,
+                                              bool reverse) {
+  if (!reverse) {
+    const int64_t idx = sched_index(k, t, warps_total);
+    return idx < nslices ? idx : -1;
+  }
+  const int passes = (int)((nslices + warps_total - 1) / warps_total);
+  const bool has_last = passes > 0 && sched_index(passes - 1, t, warps_total) < nslices;
+  const int pass = passes - 1 - k - (has_last ? 0 : 1);
+  return pass >= 0 ? sched_index(pass, t, warps_total) : -1;
 }
 
 // ---------------------------------------------------------------------------

@@ -77,6 +77,7 @@ struct Sell {
   DevBuf vals;       // vdtype[nent * B * B]
   DevBuf perm;       // int32[nrow] when rows are stored sorted by length
   DevBuf sched;      // int4[nslices]: product schedule, slices by width descending
+  DevBuf err;        // int32[1]: set by a product kernel whose bounded wait gave up
   int variant = 0;   // product kernel variant chosen by sell_autotune
   int64_t nnz = 0;   // stored entries without padding
 };
@@ -118,6 +119,11 @@ struct EpiHost {
   int kind = EPI_AXPBY;
   const void* aux0 = nullptr;
   const void* aux1 = nullptr;
+  // Walk the slices in reverse pass order (products without a fused dot;
+  // the result is the same either way): the second of two back-to-back
+  // products over one matrix then starts on the first one's most recently
+  // read slices.
+  bool reverse = false;
 };
 
 struct ReductionHost;  // defined in gbpc_common.cuh as gbpc::Reduction

@@ -94,6 +94,7 @@ __global__ void index_free_kernel(int nfree, const int32_t* __restrict__ free_id
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nfree) return;
   const int j = free_idx[i];
+  if (j != i) atomicAdd(status + 3, 1);  // not the identity selection
   if (j < 0 || j >= n) {
     atomicAdd(status + 0, 1);
   } else {
@@ -246,8 +247,10 @@ struct FsaiOp : Operator {
 
 struct SqlapOp : Operator {
   int n = 0, nfree = 0;
-  bool all_free = false;
-  Sell fwd;       // L with columns mapped to compact free indices
+  // free_indices == 0, 1, ..., n - 1: L[free, :] is L itself and compact
+  // column indices are L's, so one stored copy of L serves both products.
+  bool identity_free = false;
+  Sell fwd;       // L with columns mapped to compact free indices (not built when identity_free)
   Sell bwd;       // rows L[free, :]
   Sell bnd;       // L with only constrained columns (rhs)
   DevBuf inv_mass, wmass, tmp, index, free_idx, zeros;
@@ -255,8 +258,22 @@ struct SqlapOp : Operator {
             const DotSpec* dot, cudaStream_t st) override {
     int rc;
     if (alpha != 0.0) {
-      // tmp = (M^-1 L) x with the row scaling folded into the stored values.
-      rc = sell_spmv(fwd, vdtype, x, nullptr, tmp.p, 1.0, 0.0, guard, EpiHost{}, nullptr, st);
+      // tmp = (M^-1 L) x.  It walks its slices in reverse so that the
+      // backward product, which walks L forward, starts on the slices read
+      // last (with one copy of L they are still in L2), and the next
+      // forward product starts on the slices the backward one read last.
+      EpiHost f;
+      f.reverse = true;
+      if (identity_free) {
+        // tmp[i] = (1 / mass[i]) * (L x)[i], the reference's order
+        // (squared_laplacian.py:37-64).
+        f.kind = EPI_SQLAP_FWD;
+        f.aux0 = inv_mass.p;
+        rc = sell_spmv(bwd, vdtype, x, nullptr, tmp.p, 1.0, 0.0, guard, f, nullptr, st);
+      } else {
+        // The row scaling is folded into fwd's stored values.
+        rc = sell_spmv(fwd, vdtype, x, nullptr, tmp.p, 1.0, 0.0, guard, f, nullptr, st);
+      }
       if (rc) return rc;
     }
     EpiHost b{EPI_SQLAP_BWD, wmass.p, x};
@@ -615,10 +632,13 @@ extern "C" int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* colum
   SellBuild bd;
   bd.colmap = bmap.as<int32_t>();
   bd.row_scale = op->inv_mass.p;
-  if ((rc = sell_build(op->fwd, n, nfree, 1, offsets, columns, values, dtype, dtype, fo, st))) return fail(rc);
+  op->identity_free = nfree == n && h[3] == 0;
+  if (!op->identity_free &&
+      (rc = sell_build(op->fwd, n, nfree, 1, offsets, columns, values, dtype, dtype, fo, st)))
+    return fail(rc);
   if ((rc = sell_build(op->bwd, nfree, n, 1, offsets, columns, values, dtype, dtype, bo, st))) return fail(rc);
   if ((rc = sell_build(op->bnd, n, n, 1, offsets, columns, values, dtype, dtype, bd, st))) return fail(rc);
-  if ((rc = sell_autotune(op->fwd, dtype, st))) return fail(rc);
+  if (!op->identity_free && (rc = sell_autotune(op->fwd, dtype, st))) return fail(rc);
   if ((rc = sell_autotune(op->bwd, dtype, st))) return fail(rc);
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {

@@ -323,6 +323,8 @@ static int build_schedule(Sell& s, cudaStream_t st) {
   }
   int rc = s.sched.alloc(sizeof(int32_t) * tasks.size());
   if (rc) return rc;
+  if ((rc = s.err.alloc(sizeof(int32_t)))) return rc;
+  GBPC_CUDA_TRY(cudaMemsetAsync(s.err.p, 0, sizeof(int32_t), st));
   GBPC_CUDA_TRY(cudaMemcpyAsync(s.sched.p, tasks.data(), sizeof(int32_t) * tasks.size(),
                                 cudaMemcpyHostToDevice, st));
   GBPC_CUDA_TRY(cudaStreamSynchronize(st));
@@ -515,7 +517,7 @@ int sell_spmv(const Sell& m, int adtype, const void* x, const void* y, void* z, 
 
 // Kernel variants timed by the autotuner (scalar rows; must match
 // launch_variant in gbpc_spmv.cuh).
-constexpr int kNumVariants = 5;
+constexpr int kNumVariants = 6;
 
 // The software-pipelined variant is the default: inside Krylov iterations
 // (matrix streamed from HBM, input vector warm) it was the fastest or within
@@ -566,6 +568,7 @@ int sell_autotune(Sell& m, int adtype, cudaStream_t st) {
   for (int v = 0; v < kNumVariants && !rc; ++v) {
     ms[v] = 1e30f;
     if (blocked && v != 0 && v != 4) continue;
+    if (v == 5) continue;  // the bulk-copy variant runs only when GBPC_SPMV_VARIANT=5 selects it
     m.variant = v;
     for (int w = 0; w < 2 && !rc; ++w)
       rc = sell_spmv(m, adtype, x.p, nullptr, z.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);

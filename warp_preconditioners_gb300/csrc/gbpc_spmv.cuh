@@ -111,9 +111,9 @@ sell_spmv_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, i
   // mix of wide and narrow slices, and the slowest warp, which the kernel
   // waits for, carries close to the average work.
   const int t = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
-  for (int i = 0; (int64_t)i * warps_total < m.nslices; ++i) {
-    const int64_t idx = sched_index(i, t, warps_total);
-    if (idx >= m.nslices) break;  // later passes lie further out
+  for (int i = 0;; ++i) {
+    const int64_t idx = warp_slice(i, t, warps_total, m.nslices, !DOT && m.reverse);
+    if (idx < 0) break;  // later passes lie further out
     const SliceTask task = load_task(m.sched, idx);
     const int row = task.s * kSlice + lane;
     const int64_t base = task.base;
@@ -277,16 +277,17 @@ sell_spmv_pipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A be
   // before the wait on the previous kernel: under programmatic dependent
   // launch these loads overlap that kernel's tail.  Only x, y and the guard
   // come from the previous kernel.
-  const int64_t idx = sched_index(0, t, warps_total);
-  const bool any = idx < m.nslices;
+  const bool rev = !DOT && m.reverse;
+  const int64_t idx = warp_slice(0, t, warps_total, m.nslices, rev);
+  const bool any = idx >= 0;
   SliceTask cur{-1, 0, 0}, nxt{-1, 0, 0};
   int pc[CH];
   V pv[CH];
   bool have = false;  // pc/pv hold the first chunk of cur
   if (any) {
     cur = load_task(m.sched, idx);
-    const int64_t nidx = sched_index(1, t, warps_total);
-    if (nidx < m.nslices) nxt = load_task(m.sched, nidx);
+    const int64_t nidx = warp_slice(1, t, warps_total, m.nslices, rev);
+    if (nidx >= 0) nxt = load_task(m.sched, nidx);
     if (run) {
       load_chunk<V, CH>(m, cur, 0, lane, pc, pv);
       have = true;
@@ -330,8 +331,8 @@ sell_spmv_pipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A be
       if (nxt.s < 0) break;
       cur = nxt;
       ++i;
-      const int64_t nidx = sched_index(i + 1, t, warps_total);
-      nxt = nidx < m.nslices ? load_task(m.sched, nidx) : SliceTask{-1, 0, 0};
+      const int64_t nidx = warp_slice(i + 1, t, warps_total, m.nslices, rev);
+      nxt = nidx >= 0 ? load_task(m.sched, nidx) : SliceTask{-1, 0, 0};
     }
   }
   if (DOT) reduce_and_finalize(red, dot_part);
@@ -446,6 +447,267 @@ sell_spmv_bpipe_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A b
   if (DOT) reduce_and_finalize(red, dot_part);
 }
 
+// ---------------------------------------------------------------------------
+// Scalar rows with the matrix streamed by the bulk-copy engine.
+//
+// A slice's entries are contiguous (column-major inside the slice), so a
+// chunk of CH entries per lane is one block of 128 CH bytes of columns and
+// one of 32 CH sizeof(V) bytes of values.  Each warp owns a ring of NS
+// shared-memory stages; lane 0 keeps the next NS chunks of the warp's slice
+// sequence in flight with cp.async.bulk (completion counted in bytes on an
+// mbarrier per stage), so the DRAM stream no longer costs registers or
+// waits on the warp.  The warp reads a stage into registers, hands it back
+// to the copy engine at once, issues that chunk's x gathers, and only then
+// multiplies the previous chunk, whose gathers have been in flight for a
+// whole step.  Rows still sum their entries in storage order, slices are
+// finished in the schedule order of the other variants and the grid is the
+// same, so results (fused dot included) are identical to theirs bit for bit.
+// Every mbarrier wait is bounded: a wait that gives up sets *m.err, waits
+// (bounded) for the warp's copies in flight and leaves the kernel.
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes,
+                                             uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+constexpr int kBulkCH = 4;                 // entries per lane per stage
+constexpr int kBulkStageBytesMax = 6144;   // shared memory per warp for its ring
+constexpr uint32_t kBulkSpinLimit = 1u << 24;  // try_wait rounds before giving up
+
+template <typename V>
+struct BulkCfg {
+  static constexpr int kColBytes = kBulkCH * kSlice * 4;
+  static constexpr int kValBytes = kBulkCH * kSlice * (int)sizeof(V);
+  static constexpr int kStage = kColBytes + kValBytes;
+  static constexpr int NS = kBulkStageBytesMax / kStage;  // 4 (double), 6 (float), 8 (bf16)
+  static constexpr int kWarpBytes = NS * kStage;
+  static constexpr size_t kSmem = (size_t)(kThreads / 32) * (kWarpBytes + NS * 8);
+};
+
+// The warp's chunk sequence: its slices in schedule order, CH entries of
+// each at a time, slices of width 0 skipped (they have no entries to copy).
+struct ChunkCursor {
+  int i;          // schedule pass of the current slice
+  SliceTask task;
+  int k0;
+  bool done;
+};
+
+template <typename V>
+__device__ __forceinline__ void cursor_seek(ChunkCursor& c, const SellView<V>& m, int t, int W,
+                                            bool rev) {
+  // From pass c.i onward, the first slice with entries.
+  while (true) {
+    const int64_t idx = warp_slice(c.i, t, W, m.nslices, rev);
+    if (idx < 0) {
+      c.done = true;
+      return;
+    }
+    c.task = load_task(m.sched, idx);
+    c.k0 = 0;
+    if (c.task.width > 0) return;
+    ++c.i;
+  }
+}
+
+template <typename V>
+__device__ __forceinline__ void cursor_next(ChunkCursor& c, const SellView<V>& m, int t, int W,
+                                            bool rev) {
+  c.k0 += kBulkCH;
+  if (c.k0 < c.task.width) return;
+  ++c.i;
+  cursor_seek(c, m, t, W, rev);
+}
+
+template <typename V>
+__device__ __forceinline__ void issue_chunk(const ChunkCursor& c, const SellView<V>& m,
+                                            unsigned char* stage, uint64_t* bar) {
+  using Cfg = BulkCfg<V>;
+  const int nk = min(kBulkCH, c.task.width - c.k0);
+  const int64_t first = c.task.base + (int64_t)c.k0 * kSlice;
+  const uint32_t cb = (uint32_t)nk * kSlice * 4;
+  const uint32_t vb = (uint32_t)nk * kSlice * (uint32_t)sizeof(V);
+  mbar_arrive_expect_tx(bar, cb + vb);
+  bulk_to_smem(stage, m.cols + first, cb, bar);
+  bulk_to_smem(stage + Cfg::kColBytes, m.vals + first, vb, bar);
+}
+
+template <typename V, typename A, int EPI, bool DOT, bool UNIT = false>
+__global__ void __launch_bounds__(kThreads, 1)
+sell_spmv_bulk_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A beta, int flags,
+                      const int* guard, EpiDev<A> ep, Reduction red) {
+  using Cfg = BulkCfg<V>;
+  constexpr int NS = Cfg::NS;
+  extern __shared__ __align__(128) unsigned char bulk_smem[];
+  const bool run =
+      UNIT || (EPI == EPI_TRI_LOWER || EPI == EPI_TRI_UPPER) || !(flags & F_ALPHA_ZERO);
+  const bool alpha_one = UNIT || (flags & F_ALPHA_ONE) != 0;
+  const bool beta_zero = UNIT || (flags & F_BETA_ZERO) != 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int W = gridDim.x * (kThreads / 32);
+  const int t = warp * gridDim.x + blockIdx.x;
+  const bool rev = !DOT && m.reverse;
+  unsigned char* ring = bulk_smem + (size_t)warp * Cfg::kWarpBytes;
+  uint64_t* bars =
+      reinterpret_cast<uint64_t*>(bulk_smem + (size_t)(kThreads / 32) * Cfg::kWarpBytes) + warp * NS;
+
+  // The matrix is not written while a solve runs, so the ring is filled
+  // before the wait on the previous kernel (see sell_spmv_pipe_kernel).
+  ChunkCursor prod{0, SliceTask{-1, 0, 0}, 0, false};
+  uint32_t issued = 0;  // chunks handed to the copy engine (uniform over the warp)
+  if (run) {
+    if (lane == 0) {
+#pragma unroll
+      for (int st = 0; st < NS; ++st) mbar_init(bars + st, 1);
+      fence_mbar_init();
+    }
+    __syncwarp();
+    cursor_seek(prod, m, t, W, rev);
+    for (int st = 0; st < NS && !prod.done; ++st) {
+      if (lane == 0) issue_chunk(prod, m, ring + (size_t)st * Cfg::kStage, bars + st);
+      cursor_next(prod, m, t, W, rev);
+      ++issued;
+    }
+  }
+  pdl_wait();
+  pdl_launch_dependents();
+  bool off = guard_off(guard);
+  double dot_part = 0.0;
+  bool failed = false;
+  uint32_t q = 0;  // chunks consumed
+  // Pending chunk: values and gathered x of the chunk read last step.
+  V pv[kBulkCH];
+  A px[kBulkCH];
+  int pn = 0;          // its entry count (0: none pending)
+  bool plast = false;  // it is the last chunk of its slice
+  int prow = 0;        // row (of the slice) it belongs to
+  A acc = A(0);
+  auto multiply_pending = [&]() {
+#pragma unroll
+    for (int j = 0; j < kBulkCH; ++j)
+      if (j < pn) acc = fma_t<A>(widen<A, V>(pv[j]), px[j], acc);
+    if (plast) {
+      A a1[1] = {acc};
+      spmv_finish<1, V, A, EPI, DOT>(m, prow, a1, y, z, alpha, beta, run, alpha_one, beta_zero,
+                                     ep, red, dot_part);
+      acc = A(0);
+    }
+    pn = 0;
+  };
+  if (!off) {
+    for (int i = 0;; ++i) {
+      const int64_t idx = warp_slice(i, t, W, m.nslices, rev);
+      if (idx < 0) break;
+      const SliceTask task = load_task(m.sched, idx);
+      const int row = task.s * kSlice + lane;
+      if (!run || task.width == 0) {
+        if (pn) multiply_pending();
+        A a1[1] = {A(0)};
+        spmv_finish<1, V, A, EPI, DOT>(m, row, a1, y, z, alpha, beta, run, alpha_one, beta_zero,
+                                       ep, red, dot_part);
+        continue;
+      }
+      for (int k0 = 0; k0 < task.width; k0 += kBulkCH, ++q) {
+        const int st = (int)(q % NS);
+        const uint32_t parity = (q / NS) & 1u;
+        uint32_t spins = 0;
+        while (!mbar_try_wait(bars + st, parity)) {
+          if (++spins == kBulkSpinLimit) {
+            failed = true;
+            break;
+          }
+        }
+        if (__any_sync(0xffffffffu, failed)) {
+          failed = true;
+          break;
+        }
+        const unsigned char* sp = ring + (size_t)st * Cfg::kStage;
+        const int32_t* sc = reinterpret_cast<const int32_t*>(sp);
+        const V* sv = reinterpret_cast<const V*>(sp + Cfg::kColBytes);
+        const int nk = min(kBulkCH, task.width - k0);
+        int c[kBulkCH];
+        V v[kBulkCH];
+#pragma unroll
+        for (int j = 0; j < kBulkCH; ++j) {
+          c[j] = j < nk ? sc[j * kSlice + lane] : -1;
+          v[j] = j < nk ? sv[j * kSlice + lane] : static_cast<V>(0.0f);
+        }
+        // Stage read: order those reads before the copy engine's next write,
+        // then hand the stage back.
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (!prod.done) {
+          if (lane == 0) issue_chunk(prod, m, ring + (size_t)st * Cfg::kStage, bars + st);
+          cursor_next(prod, m, t, W, rev);
+          ++issued;
+        }
+        A xv[kBulkCH];
+#pragma unroll
+        for (int j = 0; j < kBulkCH; ++j) xv[j] = (c[j] >= 0) ? __ldg(x + c[j]) : A(0);
+        if (pn) multiply_pending();
+#pragma unroll
+        for (int j = 0; j < kBulkCH; ++j) {
+          pv[j] = v[j];
+          px[j] = xv[j];
+        }
+        pn = nk;
+        plast = k0 + kBulkCH >= task.width;
+        prow = row;
+      }
+      if (failed) break;
+    }
+    if (!failed && pn) multiply_pending();
+  }
+  if (failed || off) {
+    // Leave no copy running into this CTA's shared memory: wait (bounded)
+    // for every chunk issued and not yet consumed.
+    if (failed && lane == 0) atomicExch(m.err, 1);
+    if (run) {
+      for (uint32_t r = q; r < issued; ++r) {
+        const int st = (int)(r % NS);
+        uint32_t spins = 0;
+        while (!mbar_try_wait(bars + st, (r / NS) & 1u) && ++spins < kBulkSpinLimit) {
+        }
+      }
+    }
+    if (off) return;
+  }
+  if (DOT) reduce_and_finalize(red, dot_part);
+}
+
 // Launch configuration of a variant: CTAs resident per SM times SMs, with
 // slices spread over the warps by a grid stride.
 // Every variant launches the same grid (one 1024-thread CTA per SM at most),
@@ -469,15 +731,30 @@ static int spmv_flags(double alpha, double beta) {
 }
 
 // Product kernel variants for scalar rows: entries loaded per chunk 8, 16,
-// 4, 3 on each of two slices at once, and 4 software-pipelined; all have a
-// 64-register budget (one 1024-thread CTA per SM).  Blocked rows use one
-// variant.
-constexpr int kNumVariants = 5;
+// 4, 3 on each of two slices at once, 4 software-pipelined, and 5 streamed
+// by the bulk-copy engine; all have a 64-register budget (one 1024-thread
+// CTA per SM).  Blocked rows use one variant.
+constexpr int kNumVariants = 6;
 
 // Products with alpha == 1 and beta == 0 (all of the Krylov loops') run an
 // instantiation that knows it: no scaling or y term is issued (an FP64
 // instruction costs its issue slot even with every lane predicated off).
 constexpr int kUnitFlags = F_ALPHA_ONE | F_BETA_ZERO;
+
+template <typename V, typename A, int EPI, bool DOT, bool UNIT>
+static void launch_bulk(const SellView<V>& view, const void* x, const void* y, void* z,
+                        double alpha, double beta, int flags, const int* guard,
+                        const EpiDev<A>& e, const Reduction& red, int nslices, cudaStream_t st) {
+  auto kern = sell_spmv_bulk_kernel<V, A, EPI, DOT, UNIT>;
+  static bool ready = false;  // the opt-in shared memory size, once per instantiation
+  if (!ready) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)BulkCfg<V>::kSmem);
+    ready = true;
+  }
+  launch_k(kern, spmv_grid(nslices, 1), kThreads, BulkCfg<V>::kSmem, st, view, (const A*)x,
+           (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e, red);
+}
 
 template <int B, typename V, typename A, int EPI, bool DOT, int CH, int MINB>
 static void launch_one(const SellView<V>& view, const void* x, const void* y, void* z,
@@ -526,6 +803,14 @@ static void launch_variant(int variant, const SellView<V>& view, const void* x, 
                    st, view, (const A*)x, (const A*)y, (A*)z, (A)alpha, (A)beta, flags, guard, e,
                    red);
         return;
+      case 5:
+        if (flags == kUnitFlags)
+          launch_bulk<V, A, EPI, DOT, true>(view, x, y, z, alpha, beta, flags, guard, e, red,
+                                            nslices, st);
+        else
+          launch_bulk<V, A, EPI, DOT, false>(view, x, y, z, alpha, beta, flags, guard, e, red,
+                                             nslices, st);
+        return;
       default:
         break;
     }
@@ -554,7 +839,7 @@ static void launch_spmv(const Sell& m, const void* x, const void* y, void* z, do
                         cudaStream_t st) {
   SellView<V> view{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
                    m.vals.as<V>(), m.perm.p ? m.perm.as<int32_t>() : nullptr,
-                   m.sched.as<int4>()};
+                   m.sched.as<int4>(), ep.reverse ? 1 : 0, m.err.as<int>()};
   EpiDev<A> e{(const A*)ep.aux0, (const A*)ep.aux1};
   const int flags = spmv_flags(alpha, beta);
   if (red.w != nullptr)
@@ -588,6 +873,12 @@ static int dispatch_epi(const Sell& m, const void* x, const void* y, void* z, do
     case EPI_SQLAP_BWD:
       if constexpr (B == 1 && std::is_same<V, A>::value) {
         launch_spmv<1, V, A, EPI_SQLAP_BWD>(m, x, y, z, alpha, beta, guard, ep, red, st);
+        return GBPC_OK;
+      }
+      break;
+    case EPI_SQLAP_FWD:
+      if constexpr (B == 1 && std::is_same<V, A>::value) {
+        launch_spmv<1, V, A, EPI_SQLAP_FWD>(m, x, y, z, alpha, beta, guard, ep, red, st);
         return GBPC_OK;
       }
       break;

@@ -173,9 +173,10 @@ class FSAI(LinearOperator):
     def quality(self, A=None, probes=4, seed=17):
         """Rademacher estimate of ``||G A G^T - I||_F / sqrt(n)`` with fixed
         random probes (fsai_reuse.py:248-279): a diagnostic, not a bound on
-        conditioning or iterations.  The probes come from torch's generator,
-        so a seed does not give the reference's probe vectors.  Allocates
-        and synchronises; not capturable."""
+        conditioning or iterations.  Probe p is the reference's seeded
+        stream (``rand_init(seed + p, i)``, fsai_reuse.py:143-147) drawn on
+        the device; the products, the subtraction and the float64 dot run in
+        libgbpc.  Allocates and synchronises once; not capturable."""
         if isinstance(probes, bool) or not isinstance(probes, int) or probes < 1:
             raise ValueError("probes must be a positive integer")
         A = self.source if A is None else A
@@ -188,19 +189,26 @@ class FSAI(LinearOperator):
         from .linear import aslinearoperator
 
         dt = A.scalar_type
+        code = _lib.dtype_code(dt)
         g_op, gt_op = _product_op(self.G, dt), _product_op(self.GT, dt)
         a_op = aslinearoperator(A)
         x, y, z, w = (torch.empty(n, dtype=dt, device=A.device) for _ in range(4))
-        gen = torch.Generator()
-        total = 0.0
+        work = torch.empty(_lib.load().gbpc_vec_dot_work_size(), dtype=torch.float64,
+                           device=A.device)
+        dots = torch.empty(probes, dtype=torch.float64, device=A.device)
+        st = _lib.stream(A.device)
         for p in range(probes):
-            gen.manual_seed(seed + p)
-            x.copy_(torch.randint(0, 2, (n,), generator=gen).to(dt) * 2 - 1)
+            _lib.call("gbpc_rademacher", n, seed + p, code, _lib.ptr(x), st)
             gt_op.apply(x, None, y, 1.0, 0.0, A.device)
             a_op.matvec(y, None, z, 1.0, 0.0)
             g_op.apply(z, None, w, 1.0, 0.0, A.device)
-            w -= x
-            total += float(torch.dot(w, w))
+            _lib.call("gbpc_vec_axpby", n, code, 1.0, _lib.ptr(w), -1.0, _lib.ptr(x),
+                      _lib.ptr(w), st)
+            _lib.call("gbpc_vec_dot", n, code, _lib.ptr(w), _lib.ptr(w), _lib.ptr(work),
+                      ctypes.c_void_p(dots.data_ptr() + 8 * p), st)
+        total = 0.0
+        for d in dots.tolist():  # the reference adds the probes' dots in order on the host
+            total += d
         return (total / (probes * max(n, 1))) ** 0.5
 
     def _apply(self, x, y, z, alpha, beta):

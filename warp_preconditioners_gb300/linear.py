@@ -135,13 +135,147 @@ class Solver:
         return self.nit, self.rr, self.atol_sq
 
 
+class _Vec:
+    """libgbpc vector kernels on flat device vectors of one dtype."""
+
+    def __init__(self, n, dtype, device):
+        self.n = n
+        self.code = _lib.dtype_code(dtype)
+        self.stream = _lib.stream(device)
+        self.work = torch.empty(_lib.load().gbpc_vec_dot_work_size(), dtype=torch.float64,
+                                device=device)
+        self.out = torch.zeros(4, dtype=torch.float64, device=device)
+
+    def axpby(self, alpha, x, beta, y, z):
+        _lib.call("gbpc_vec_axpby", self.n, self.code, float(alpha),
+                  _lib.ptr(x) if alpha != 0.0 else None, float(beta),
+                  _lib.ptr(y) if beta != 0.0 else None, _lib.ptr(z), self.stream)
+
+    def dot(self, x, y, slot):
+        _lib.call("gbpc_vec_dot", self.n, self.code, _lib.ptr(x), _lib.ptr(y),
+                  _lib.ptr(self.work), ctypes.c_void_p(self.out.data_ptr() + 8 * slot),
+                  self.stream)
+
+    def read(self, count):
+        return self.out[:count].tolist()
+
+
+def _host_krylov(method, A, M, b, x, tol, atol, maxiter):
+    """CG / CR stepped from the host, for operators without a libgbpc handle
+    (any ``LinearOperator(shape, dtype, device, matvec)``) and for float32
+    systems.  Every vector update and dot product runs in libgbpc kernels on
+    the device; the host reads the dot products (two synchronisations per
+    iteration) to form the scalars.  Same recurrences and stopping rule as
+    the device loop (warp.optim.linear: r.r <= max(atol, tol |b|)^2 or
+    maxiter); float64 dot accumulation for every vector dtype."""
+    bf, xf = _flat(b), _flat(x)
+    n = bf.numel()
+    dev = bf.device
+    v = _Vec(n, bf.dtype, dev)
+    r, z, p, Ap = (torch.empty_like(bf) for _ in range(4))
+
+    def apply(op, src, dst):
+        op.matvec(src.view(b.shape), dst.view(b.shape), dst.view(b.shape), 1.0, 0.0)
+
+    def precondition(src, dst):
+        if M is None:
+            v.axpby(1.0, src, 0.0, None, dst)
+        else:
+            apply(M, src, dst)
+
+    if maxiter <= 0:
+        maxiter = n
+    A.matvec(x, b, r.view(b.shape), -1.0, 1.0)  # r = b - A x
+    v.dot(bf, bf, 0)
+    v.dot(r, r, 1)
+    precondition(r, z)
+    v.axpby(1.0, z, 0.0, None, p)
+    if method == "cg":
+        v.dot(r, z, 2)
+        bb, rr, rz = v.read(3)
+    else:
+        Az, y = torch.empty_like(bf), torch.empty_like(bf)
+        apply(A, z, Az)
+        v.axpby(1.0, Az, 0.0, None, Ap)
+        v.dot(z, Az, 2)
+        bb, rr, rz = v.read(3)
+    atol_sq = max(atol, tol * math.sqrt(bb)) ** 2
+    it = 0
+    while rr > atol_sq and it < maxiter:
+        if method == "cg":
+            apply(A, p, Ap)
+            v.dot(p, Ap, 0)
+            (pap,) = v.read(1)
+            alpha = rz / pap
+            v.axpby(alpha, p, 1.0, xf, xf)
+            v.axpby(-alpha, Ap, 1.0, r, r)
+            precondition(r, z)
+            v.dot(r, r, 0)
+            v.dot(r, z, 1)
+            rr, rz_new = v.read(2)
+            beta = rz_new / rz
+            rz = rz_new
+            v.axpby(1.0, z, beta, p, p)
+        else:
+            precondition(Ap, y)
+            v.dot(Ap, y, 0)
+            (apy,) = v.read(1)
+            alpha = rz / apy
+            v.axpby(alpha, p, 1.0, xf, xf)
+            v.axpby(-alpha, Ap, 1.0, r, r)
+            v.axpby(-alpha, y, 1.0, z, z)
+            apply(A, z, Az)
+            v.dot(r, r, 0)
+            v.dot(z, Az, 1)
+            rr, rz_new = v.read(2)
+            beta = rz_new / rz
+            rz = rz_new
+            v.axpby(1.0, z, beta, p, p)
+            v.axpby(1.0, Az, beta, Ap, Ap)
+        it += 1
+    return it, rr, atol_sq
+
+
+def _cached_solver(method, A, M, use_cuda_graph) -> Solver:
+    """One Solver per (operator, preconditioner, method, graph flag), kept on
+    the operator, so repeated cg / cr calls replay the captured graph
+    instead of capturing a new one (it is rebuilt only for new b / x)."""
+    cache = A.__dict__.setdefault("_gbpc_solvers", [])
+    for entry in cache:
+        if entry[0] == method and entry[1] is M and entry[2] == bool(use_cuda_graph):
+            return entry[3]
+    s = Solver(method, A, M, use_cuda_graph)
+    cache.append((method, M, bool(use_cuda_graph), s))
+    if len(cache) > 4:
+        cache.pop(0)
+    return s
+
+
 def _solve(method, A, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph):
     if callback is not None:
         raise NotImplementedError("per-iteration callbacks are not supported; the loop runs on "
                                   "the device")
-    if b.dtype != torch.float64 or x.dtype != torch.float64:
-        raise TypeError("cg/cr run on float64 vectors")
-    s = Solver(method, A, M, use_cuda_graph)
+    A = aslinearoperator(A)
+    M = aslinearoperator(M)
+    if b.dtype != x.dtype or b.shape != x.shape:
+        raise TypeError("b and x must have the same dtype and shape")
+    if b.dtype not in (torch.float32, torch.float64):
+        raise TypeError("cg/cr run on float32 or float64 vectors")
+    if A.dtype != b.dtype or (M is not None and M.dtype != b.dtype):
+        raise TypeError("operator and vector dtypes differ")
+    tol = 1.0e-5 if tol is None else float(tol)
+    atol = 0.0 if atol is None else float(atol)
+    native = (b.dtype == torch.float64 and getattr(A, "_op", None) is not None
+              and (M is None or getattr(M, "_op", None) is not None))
+    if not native:
+        it, rr, atol_sq = _host_krylov(method, A, M, b, x, tol, atol, int(maxiter))
+        if check_every == 0:
+            dev = b.device
+            return (torch.tensor([it], dtype=torch.int32, device=dev),
+                    torch.tensor([rr], dtype=torch.float64, device=dev),
+                    torch.tensor([atol_sq], dtype=torch.float64, device=dev))
+        return it, math.sqrt(max(rr, 0.0)), math.sqrt(atol_sq)
+    s = _cached_solver(method, A, M, use_cuda_graph)
     nit, rr, atol_sq = s.run(b, x, tol, atol, maxiter)
     if check_every == 0:
         return nit.clone(), rr.clone(), atol_sq.clone()

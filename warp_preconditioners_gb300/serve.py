@@ -128,7 +128,16 @@ class HostSystem:
     n: int
     A: object                # scipy CSR: the Laplacian L, or the stiffness K
     mass: np.ndarray | None  # lumped mass (biharmonic)
-    P: object                # scipy CSR the FSAI factor approximates: L, or Q
+
+    def assembled(self):
+        """The matrix the FSAI factor approximates, assembled on the host: L,
+        or Q = alpha M + K M^-1 K.  Only for checking: resident systems
+        assemble Q on the device."""
+        if self.kind == "laplacian":
+            return self.A
+        from . import problems
+
+        return problems.biharmonic(self.A, self.mass, ALPHA)
 
 
 def host_system(kind: str, side: int) -> HostSystem:
@@ -136,10 +145,10 @@ def host_system(kind: str, side: int) -> HostSystem:
 
     if kind == "laplacian":
         L = problems.laplacian_3d(side)
-        return HostSystem(kind, side, L.shape[0], L, None, L)
+        return HostSystem(kind, side, L.shape[0], L, None)
     if kind == "biharmonic":
         _, _, K, mass = problems.tet_cube(side)
-        return HostSystem(kind, side, K.shape[0], K, mass, problems.biharmonic(K, mass, ALPHA))
+        return HostSystem(kind, side, K.shape[0], K, mass)
     raise ValueError(f"unknown system kind {kind!r}")
 
 
@@ -199,22 +208,27 @@ class ResidentSystem:
         from .batched import BatchedCG, batched_fsai, batched_sparse, batched_sqlap
         from .fsai import FSAI
         from .linear import Solver, aslinearoperator
-        from .sparse import from_scipy
+        from .sparse import from_scipy, spgemm
         from .squared_laplacian import SquaredLaplacianOperator
 
         dev = torch.device(device)
         self.key = (host.kind, host.side)
         self.n = n = host.n
         self.max_rhs = max_rhs
-        P = from_scipy(host.P, dev)
+        A = from_scipy(host.A, dev)
+        if host.kind == "laplacian":
+            P = A
+        else:
+            # Q = K diag(1 / m) K + diag(alpha m) by the device SpGEMM, equal
+            # bit for bit to the host SciPy assembly.
+            mass = torch.as_tensor(host.mass, dtype=torch.float64, device=dev)
+            P = spgemm(A, A, col_scale=1.0 / mass, add_diag=ALPHA * mass)
         self.fsai = FSAI(P, max_row_size=width, kap_tolerance=kap, max_step_size=step)
         self.fsai.source = None  # the solves need only the factor
         del P
-        A = from_scipy(host.A, dev)
         if host.kind == "laplacian":
             self.A = aslinearoperator(A)
         else:
-            mass = torch.as_tensor(host.mass, dtype=torch.float64, device=dev)
             free = torch.arange(n, dtype=torch.int32, device=dev)
             self.A = SquaredLaplacianOperator(A, mass, free, mass_weight=ALPHA)
         self.solver = Solver("cg", self.A, self.fsai)

@@ -259,3 +259,31 @@ def spgemm(A: BsrMatrix, B: BsrMatrix, col_scale=None, add_diag=None) -> BsrMatr
     _lib.call("gbpc_spgemm", *args, _lib.ptr(col), _lib.ptr(val), ctypes.byref(nnz),
               _lib.stream(dev))
     return BsrMatrix(A.nrow, B.ncol, (1, 1), off, col[:nnz.value], val[:nnz.value])
+
+
+def block_diag(mats) -> BsrMatrix:
+    """Block-diagonal concatenation of BSR matrices with the same block shape
+    and dtype (the systems of a multi-system solve): row offsets and
+    columns shifted, values concatenated; canonical when each input is."""
+    mats = list(mats)
+    if not mats:
+        raise ValueError("block_diag needs at least one matrix")
+    bs, dt, dev = mats[0].block_shape, mats[0].scalar_type, mats[0].device
+    for m in mats:
+        if m.block_shape != bs or m.scalar_type != dt or m.device != dev:
+            raise ValueError("block_diag needs one block shape, dtype and device")
+    offs, cols, vals = [torch.zeros(1, dtype=torch.int32, device=dev)], [], []
+    row0 = col0 = nz0 = 0
+    for m in mats:
+        offs.append(m.offsets[1:].to(torch.int64) + nz0)
+        cols.append(m.columns.to(torch.int64) + col0)
+        vals.append(m.values)
+        row0 += m.nrow
+        col0 += m.ncol
+        nz0 += m.nnz
+    if nz0 > 0x7fffffff or col0 > 0x7fffffff:
+        raise ValueError("block_diag result exceeds 32-bit indices")
+    off = torch.cat([o.to(torch.int32) for o in offs])
+    col = torch.cat(cols).to(torch.int32) if cols else torch.zeros(0, dtype=torch.int32, device=dev)
+    val = torch.cat(vals)
+    return BsrMatrix(row0, col0, bs, off, col, val)
