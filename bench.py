@@ -459,6 +459,8 @@ def main():
         line["batched_rhs4"] = measure_batched_rhs4(args, prob, Q, K, mass, dev, ms_per_step)
         line["f32_apply_rhs4"] = measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev,
                                                         ms_per_step)
+    if not args.no_mixed:
+        line["multi_system"] = measure_multi_system(dev)
     line["refit"] = measure_refit(args, prob, Q, dev)
     line["assembly"] = measure_assembly(prob, dev)
     if args.lifted:
@@ -773,6 +775,89 @@ def measure_refit(args, prob, Q, dev):
     refit_ms = timed(refit)
     return {"matrix": f"Q with alpha {ALPHA:g} -> {2 * ALPHA:g} (same pattern)",
             "setup_ms": setup_ms, "refit_ms": refit_ms, "setup_over_refit": setup_ms / refit_ms}
+
+
+def measure_multi_system(dev, sides=tuple(range(17, 38, 2)) + (18, 24, 30, 36, 22), tol=1e-8):
+    """Many independent smoothing systems of uneven size in one solve
+    (multi.MultiSystemSolver: block-diagonal operator and FSAI, per-system
+    scalars and stopping tests) against the same systems solved one at a
+    time with the drop-in float64 solver.  Tet cubes of the given sides
+    (4,913 to 50,653 unknowns), FSAI w8, first right-hand side, CG to `tol`;
+    operators and factors built beforehand, solve time only, CUDA-event
+    medians of 3."""
+    import torch
+
+    from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, from_scipy, linear, problems
+    from warp_preconditioners_gb300.multi import MultiSystemSolver
+    from warp_preconditioners_gb300.sparse import block_diag
+
+    systems = []
+    for side in sides:
+        verts, _, Kh, mh = problems.tet_cube(side)
+        Qh = problems.biharmonic(Kh, mh, ALPHA)
+        systems.append((from_scipy(Kh, dev), from_scipy(Qh, dev),
+                        torch.as_tensor(mh, device=dev),
+                        torch.as_tensor(problems.smoothing_rhs(verts, mh, ALPHA)[0], device=dev)))
+    sizes = [s[0].nrow for s in systems]
+
+    def timed(fn):
+        out = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return statistics.median(out), r
+
+    solo = []
+    for K, Q, m, b in systems:
+        n = K.nrow
+        op = SquaredLaplacianOperator(K, m, torch.arange(n, dtype=torch.int32, device=dev),
+                                      mass_weight=ALPHA)
+        solver = linear.Solver("cg", op, FSAI(Q, max_row_size=8))
+        x = torch.zeros(n, dtype=torch.float64, device=dev)
+        solo.append((solver, b, x))
+
+    def run_solo():
+        its = []
+        for solver, b, x in solo:
+            x.zero_()
+            nit, _, _ = solver.run(b, x, tol=tol, maxiter=100000)
+            its.append(nit)
+        return its
+
+    run_solo()
+    t_solo, its_solo = timed(run_solo)
+    Kb = block_diag([s[0] for s in systems])
+    Qb = block_diag([s[1] for s in systems])
+    mb = torch.cat([s[2] for s in systems])
+    bb = torch.cat([s[3] for s in systems]).contiguous()
+    N = Kb.nrow
+    op = SquaredLaplacianOperator(Kb, mb, torch.arange(N, dtype=torch.int32, device=dev),
+                                  mass_weight=ALPHA)
+    multi = MultiSystemSolver(op, FSAI(Qb, max_row_size=8), sizes)
+    xb = torch.zeros_like(bb)
+
+    def run_multi():
+        xb.zero_()
+        nit, _, _ = multi.run(bb, xb, tol=tol, maxiter=100000)
+        return nit
+
+    run_multi()
+    t_multi, its_multi = timed(run_multi)
+    its_solo = [int(i.item()) for i in its_solo]
+    its_multi = [int(i) for i in its_multi.cpu().tolist()]
+    S = len(sizes)
+    return {"workload": (f"{S} biharmonic smoothing systems on tet cubes of sides "
+                         f"{min(sides)}..{max(sides)} ({min(sizes)}..{max(sizes)} unknowns, "
+                         f"{N} in all), FSAI w8, CG to {tol:g}, first right-hand side"),
+            "one_at_a_time_ms": t_solo, "one_launch_ms": t_multi,
+            "one_at_a_time_solves_per_s": S * 1e3 / t_solo,
+            "one_launch_solves_per_s": S * 1e3 / t_multi, "speedup": t_solo / t_multi,
+            "iterations_one_at_a_time": its_solo, "iterations_one_launch": its_multi}
 
 
 def measure_batched_rhs4(args, prob, Q, K, mass, dev, ms_per_step):

@@ -14,7 +14,7 @@ from gpu_helpers import cuda, to_bsr, vec
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = range(5)
+VARIANTS = range(6)
 
 
 @pytest.fixture

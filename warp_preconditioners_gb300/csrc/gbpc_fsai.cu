@@ -418,10 +418,33 @@ fsai_build_kernel(BuildParams P, const int32_t* __restrict__ off, const int32_t*
 
 constexpr int kLanesWarps = 4;
 
-__host__ __device__ constexpr size_t lanes_smem_bytes(int T_size, int W, int SC, int H) {
+__host__ __device__ constexpr size_t lanes_smem_bytes(int T_size, int W, int SC, int H, int PH) {
   return ((size_t)T_size * ((size_t)H + 32 * (size_t)W) +
-          sizeof(int) * ((size_t)H + 32 * (size_t)W + 32 * (size_t)SC) + 15) &
+          sizeof(int) * ((size_t)H + 32 * (size_t)W + 32 * (size_t)SC + (size_t)PH) + 15) &
          ~(size_t)15;
+}
+
+// Membership set of the row being scored: open addressing on the column.
+__device__ __forceinline__ bool pset_has(const int* pkey, int pmask, int pbits, int c) {
+  unsigned int s = hash_col(c) >> (32 - pbits);
+  for (int probe = 0; probe <= pmask; ++probe) {
+    const int k = pkey[s];
+    if (k == c) return true;
+    if (k == kEmpty) return false;
+    s = (s + 1) & pmask;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void pset_add(int* pkey, int pmask, int pbits, int c) {
+  unsigned int s = hash_col(c) >> (32 - pbits);
+  for (int probe = 0; probe <= pmask; ++probe) {
+    if (pkey[s] == kEmpty) {
+      pkey[s] = c;
+      return;
+    }
+    s = (s + 1) & pmask;
+  }
 }
 
 template <typename T, int WMAX>
@@ -437,14 +460,17 @@ fsai_build_lanes_kernel(BuildParams P, const int32_t* __restrict__ off,
   const int W = P.width, H = P.hsize;
   const int SC = min(P.step, W);  // candidates ever used per round
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t row0 = ((int64_t)blockIdx.x * kLanesWarps + warp) * 32;
+  const int64_t row0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * 32;
   if (row0 >= P.n) return;
-  unsigned char* base = lanes_smem + (size_t)warp * lanes_smem_bytes((int)sizeof(T), W, SC, H);
+  const int PH = P.psize, pmask = PH - 1;
+  unsigned char* base =
+      lanes_smem + (size_t)warp * lanes_smem_bytes((int)sizeof(T), W, SC, H, PH);
   T* hacc = reinterpret_cast<T*>(base);  // [H]
   T* zS = hacc + H;                      // [32][W]
   int* hkey = reinterpret_cast<int*>(zS + 32 * W);  // [H]
   int* patS = hkey + H;                  // [32][W]
   int* candS = patS + 32 * W;            // [32][SC]
+  int* pkey = candS + 32 * SC;           // [PH]: support of the row being scored
   const int hmask = H - 1;
   const int i = (int)row0 + lane;
   const bool exists = i < P.n;
@@ -478,6 +504,10 @@ fsai_build_lanes_kernel(BuildParams P, const int32_t* __restrict__ off,
         hkey[s2] = kEmpty;
         hacc[s2] = T(0);
       }
+      for (int s2 = lane; s2 < PH; s2 += 32) pkey[s2] = kEmpty;
+      __syncwarp();
+      if (lane == 0)
+        for (int t = 0; t < rsize; ++t) pset_add(pkey, pmask, P.pbits, rpat[t]);
       __syncwarp();
       bool overflow = false;
       for (int q = 0; q < rsize; ++q) {
@@ -487,9 +517,7 @@ fsai_build_lanes_kernel(BuildParams P, const int32_t* __restrict__ off,
         for (int e = off[pq] + lane; e < e_end; e += 32) {
           const int c = col[e];
           if (c >= ri) continue;
-          bool member = false;
-          for (int t = 0; t < rsize; ++t) member |= (rpat[t] == c);
-          if (member) continue;
+          if (pset_has(pkey, pmask, P.pbits, c)) continue;
           const int slot = hfind_insert(hkey, hmask, P.hbits, c);
           if (slot < 0) {
             overflow = true;
@@ -1108,9 +1136,13 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
   // at 48 the per-thread factor, 10.6 KB in float64, lives in local memory).
   auto launch_lanes = [&](int H, int hbits) -> int {
     const int SC = std::min(S, W);
-    const size_t per_warp = lanes_smem_bytes((int)sizeof(T), W, SC, H);
-    const size_t smem = per_warp * kLanesWarps;
-    if (smem > (size_t)smem_optin) return launch(H, hbits, nullptr, n);
+    const size_t per_warp = lanes_smem_bytes((int)sizeof(T), W, SC, H, PH);
+    if (per_warp > (size_t)smem_optin) return launch(H, hbits, nullptr, n);
+    // Warps per CTA: up to kLanesWarps while a CTA stays within ~64 KB, so
+    // that wide rows (whose per-warp tables are large) still get several
+    // resident CTAs per SM instead of one.
+    int wpc = (int)std::min<size_t>(kLanesWarps, std::max<size_t>(1, (64 * 1024) / per_warp));
+    const size_t smem = per_warp * wpc;
     auto kern = (W <= 8) ? fsai_build_lanes_kernel<T, 8>
                 : (W <= 16) ? fsai_build_lanes_kernel<T, 16> : fsai_build_lanes_kernel<T, 48>;
     GBPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1129,7 +1161,7 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     P.overflow_count = stat + 5;
     const int64_t warps_needed = ((int64_t)n + 31) / 32;
     if (n > 0)
-      kern<<<(int)((warps_needed + kLanesWarps - 1) / kLanesWarps), 32 * kLanesWarps, smem, st>>>(
+      kern<<<(int)((warps_needed + wpc - 1) / wpc), 32 * wpc, smem, st>>>(
           P, off, col, ahat.as<T>(), ahatT.as<T>(), scale, (T)kap, (T)floor_, ell_cols, ell_vals,
           counts, stat);
     GBPC_CUDA_TRY(cudaGetLastError());

@@ -496,16 +496,13 @@ __device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
 constexpr int kBulkCH = 4;                 // entries per lane per stage
 constexpr int kBulkStageBytesMax = 6144;   // shared memory per warp for its ring
-constexpr uint32_t kBulkSpinLimit = 1u << 24;  // try_wait rounds before giving up
+constexpr uint32_t kBulkSpinLimit = 1u << 20;  // try_wait rounds before giving up
 
 template <typename V>
 struct BulkCfg {
@@ -608,17 +605,37 @@ sell_spmv_bulk_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A be
   double dot_part = 0.0;
   bool failed = false;
   uint32_t q = 0;  // chunks consumed
-  // Pending chunk: values and gathered x of the chunk read last step.
-  V pv[kBulkCH];
+  // Pending chunk: the chunk whose x gathers went out last step; its values
+  // are read from its stage when it is multiplied, and the stage goes back
+  // to the copy engine after that.
   A px[kBulkCH];
   int pn = 0;          // its entry count (0: none pending)
+  int pst = 0;         // its stage
   bool plast = false;  // it is the last chunk of its slice
   int prow = 0;        // row (of the slice) it belongs to
   A acc = A(0);
   auto multiply_pending = [&]() {
-#pragma unroll
-    for (int j = 0; j < kBulkCH; ++j)
-      if (j < pn) acc = fma_t<A>(widen<A, V>(pv[j]), px[j], acc);
+    // Exactly pn multiply-adds, in entry order: pn is the same on every lane,
+    // so a slice's short last chunk issues no predicated-off FP64
+    // instructions (each would still take an issue slot).
+    static_assert(kBulkCH == 4, "the cases below spell out chunks of 4");
+    const V* sv = reinterpret_cast<const V*>(ring + (size_t)pst * Cfg::kStage + Cfg::kColBytes) +
+                  lane;
+    if (pn == 4) {
+      acc = fma_t<A>(widen<A, V>(sv[0]), px[0], acc);
+      acc = fma_t<A>(widen<A, V>(sv[kSlice]), px[1], acc);
+      acc = fma_t<A>(widen<A, V>(sv[2 * kSlice]), px[2], acc);
+      acc = fma_t<A>(widen<A, V>(sv[3 * kSlice]), px[3], acc);
+    } else if (pn == 3) {
+      acc = fma_t<A>(widen<A, V>(sv[0]), px[0], acc);
+      acc = fma_t<A>(widen<A, V>(sv[kSlice]), px[1], acc);
+      acc = fma_t<A>(widen<A, V>(sv[2 * kSlice]), px[2], acc);
+    } else if (pn == 2) {
+      acc = fma_t<A>(widen<A, V>(sv[0]), px[0], acc);
+      acc = fma_t<A>(widen<A, V>(sv[kSlice]), px[1], acc);
+    } else {
+      acc = fma_t<A>(widen<A, V>(sv[0]), px[0], acc);
+    }
     if (plast) {
       A a1[1] = {acc};
       spmv_finish<1, V, A, EPI, DOT>(m, prow, a1, y, z, alpha, beta, run, alpha_one, beta_zero,
@@ -626,6 +643,14 @@ sell_spmv_bulk_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A be
       acc = A(0);
     }
     pn = 0;
+    // Every lane's reads of the stage precede the refill (the warp barrier
+    // is the release / acquire the mbarrier pipelines rely on).
+    __syncwarp();
+    if (!prod.done) {
+      if (lane == 0) issue_chunk(prod, m, ring + (size_t)pst * Cfg::kStage, bars + pst);
+      cursor_next(prod, m, t, W, rev);
+      ++issued;
+    }
   };
   if (!off) {
     for (int i = 0;; ++i) {
@@ -654,36 +679,20 @@ sell_spmv_bulk_kernel(SellView<V> m, const A* x, const A* y, A* z, A alpha, A be
           failed = true;
           break;
         }
-        const unsigned char* sp = ring + (size_t)st * Cfg::kStage;
-        const int32_t* sc = reinterpret_cast<const int32_t*>(sp);
-        const V* sv = reinterpret_cast<const V*>(sp + Cfg::kColBytes);
+        const int32_t* sc =
+            reinterpret_cast<const int32_t*>(ring + (size_t)st * Cfg::kStage) + lane;
         const int nk = min(kBulkCH, task.width - k0);
-        int c[kBulkCH];
-        V v[kBulkCH];
-#pragma unroll
-        for (int j = 0; j < kBulkCH; ++j) {
-          c[j] = j < nk ? sc[j * kSlice + lane] : -1;
-          v[j] = j < nk ? sv[j * kSlice + lane] : static_cast<V>(0.0f);
-        }
-        // Stage read: order those reads before the copy engine's next write,
-        // then hand the stage back.
-        fence_proxy_async_smem();
-        __syncwarp();
-        if (!prod.done) {
-          if (lane == 0) issue_chunk(prod, m, ring + (size_t)st * Cfg::kStage, bars + st);
-          cursor_next(prod, m, t, W, rev);
-          ++issued;
-        }
         A xv[kBulkCH];
 #pragma unroll
-        for (int j = 0; j < kBulkCH; ++j) xv[j] = (c[j] >= 0) ? __ldg(x + c[j]) : A(0);
+        for (int j = 0; j < kBulkCH; ++j) {
+          const int c = j < nk ? sc[j * kSlice] : -1;
+          xv[j] = c >= 0 ? __ldg(x + c) : A(0);
+        }
         if (pn) multiply_pending();
 #pragma unroll
-        for (int j = 0; j < kBulkCH; ++j) {
-          pv[j] = v[j];
-          px[j] = xv[j];
-        }
+        for (int j = 0; j < kBulkCH; ++j) px[j] = xv[j];
         pn = nk;
+        pst = st;
         plast = k0 + kBulkCH >= task.width;
         prow = row;
       }
