@@ -362,6 +362,13 @@ int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_graph, int un
 int gbpc_solver_run(gbpc_solver* solver, const double* b, double* x, double tol, double atol,
                     int maxiter, int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
                     void* stream);
+
+/* Residual history of the solver's next runs: hist[k] = |r_k|_2 (the
+ * recursive residual the stopping test reads) for every iteration k <
+ * hist_len, hist[0] the initial residual; hist_len = 0 turns it off.  The
+ * iterates do not change.  Replaces the reference's diagnostic patch of
+ * Warp's loop driver (benchmarks/residual_history.py:22-46). */
+int gbpc_solver_set_history(gbpc_solver* solver, double* hist, int hist_len);
 int gbpc_solver_destroy(gbpc_solver* solver);
 /* Device bytes of the solver's Krylov state (work vectors, scalars). */
 int gbpc_solver_device_bytes(const gbpc_solver* solver, size_t* bytes_host);

@@ -88,6 +88,7 @@ _SIGNATURES = {
     "gbpc_solver_create": [_int, _vp, _vp, _int, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_solver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_solver_destroy": [_vp],
+    "gbpc_solver_set_history": [_vp, _vp, _int],
     "gbpc_solver_device_bytes": [_vp, _szp],
     "gbpc_gmres_create": [_vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_gmres_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _int, _vp, _vp, _vp, _vp],

@@ -1123,6 +1123,7 @@ extern "C" int gbpc_bsolver_create(gbpc_bop* A, gbpc_bop* M, int unroll, int max
 extern "C" int gbpc_bsolver_run(gbpc_bsolver* h, int k, const void* B, void* X, double tol,
                                 double atol, int maxiter, int32_t* nit_dev, double* rr_dev,
                                 void* stream) {
+  NvtxRange nvtx_range("gbpc_bsolver_run");
   if (!h || k < 1 || k > h->s.max_rhs || !B || !X) {
     gbpc_set_error("gbpc_bsolver_run: bad arguments (k must be 1..%d)", h ? h->s.max_rhs : kB);
     return GBPC_ERR_ARG;

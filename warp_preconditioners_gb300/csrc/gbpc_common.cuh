@@ -131,6 +131,9 @@ struct KrylovScalars {
   unsigned long long cond_handle;  // cudaGraphConditionalHandle (0 = none)
   double tol;
   double atol;
+  double* hist;    // residual history: hist[k] = |r_k| for k < hist_len (nullptr: none)
+  int hist_len;
+  int pad2;
 };
 
 // What the last CTA does with a finished reduction.
@@ -223,6 +226,7 @@ __device__ __forceinline__ void finalize(const Reduction& red, double total) {
       const double a = fmax(ks->atol, ks->tol * sqrt(ks->bb));
       ks->atol_sq = a * a;
       ks->it = 0;
+      if (ks->hist && ks->hist_len > 0) ks->hist[0] = sqrt(total);
       set_active(ks);
       break;
     }
@@ -236,6 +240,8 @@ __device__ __forceinline__ void finalize(const Reduction& red, double total) {
       break;
     case FIN_RR:
       ks->rr = total;
+      // The iteration count is advanced later in the same iteration.
+      if (ks->hist && ks->it + 1 < ks->hist_len) ks->hist[ks->it + 1] = sqrt(total);
       break;
     case FIN_CG_BETA:
       ks->rz_new = total;

@@ -1215,6 +1215,7 @@ extern "C" int gbpc_fsai_setup(int n, const int32_t* offsets, const int32_t* col
                                double kap_tolerance, double pivot_floor, int32_t* ell_cols,
                                void* ell_vals, int32_t* row_counts, void* scale,
                                int32_t* status_host, void* stream) {
+  NvtxRange nvtx_range("gbpc_fsai_setup");
   if (n < 0 || !offsets || (n > 0 && (!columns || !values || !ell_cols || !ell_vals ||
                                       !row_counts || !scale))) {
     gbpc_set_error("gbpc_fsai_setup: null or negative argument");
@@ -1441,6 +1442,7 @@ extern "C" int gbpc_fsai_refit(int n, const int32_t* a_off, const int32_t* a_col
                                const void* a_val, int dtype, const int32_t* g_off,
                                const int32_t* g_col, int width, double pivot_floor, void* out,
                                int factor_dtype, int32_t* status_host, void* stream) {
+  NvtxRange nvtx_range("gbpc_fsai_refit");
   if (n < 0 || width < 1 || width > 64 || !status_host ||
       (n > 0 && (!a_off || !a_col || !a_val || !g_off || !g_col || !out)) ||
       !(pivot_floor > 0.0 && pivot_floor < 1.0)) {

@@ -868,6 +868,7 @@ extern "C" int gbpc_gmres_create(gbpc_op* A, gbpc_op* M, int restart, void* stre
 extern "C" int gbpc_gmres_run(gbpc_gmres* h, const double* b, double* x, double tol, double atol,
                               int maxiter, int use_graph, int32_t* nit_dev, double* res_dev,
                               double* target_dev, void* stream) {
+  NvtxRange nvtx_range("gbpc_gmres_run");
   if (!h || !b || !x) {
     gbpc_set_error("gbpc_gmres_run: bad arguments");
     return GBPC_ERR_ARG;

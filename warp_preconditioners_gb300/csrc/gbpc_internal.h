@@ -7,9 +7,20 @@
 #include <memory>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gbpc.h"
 
 namespace gbpc {
+
+// An NVTX range around a setup, apply or solve entry point (visible in
+// Nsight timelines; costs nothing measurable when no tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 constexpr int kMaxCtas = 152 * 8;  // partial-sum capacity of every reduction buffer
 

@@ -136,13 +136,15 @@ __global__ void widen_copy_kernel(int64_t n, const float* z32, double* p) {
 }
 
 __global__ void set_scalars_kernel(KrylovScalars* ks, double tol, double atol, int maxiter,
-                                   unsigned long long handle) {
+                                   unsigned long long handle, double* hist, int hist_len) {
   ks->tol = tol;
   ks->atol = atol;
   ks->maxiter = maxiter;
   ks->it = 0;
   ks->active = 1;
   ks->cond_handle = handle;
+  ks->hist = hist;
+  ks->hist_len = hist ? hist_len : 0;
 }
 
 __global__ void copy_outputs_kernel(const KrylovScalars* ks, int32_t* nit, double* rr,
@@ -169,6 +171,8 @@ struct Solver {
   int64_t n = 0;
   bool use_graph = true;
   int unroll = 8;  // iterations per pass of the device loop (measured: 1 -> 8 saves ~4 us/iteration)
+  double* hist = nullptr;  // residual history of the next runs (gbpc_solver_set_history)
+  int hist_len = 0;
   bool use_pdl = true;  // programmatic dependent launches inside the loop body
   DevBuf r, z, p, Ap, Az, y, ks, zeros;
   ReduceBuf rb;
@@ -400,11 +404,12 @@ struct Solver {
         }
         if (rc) return rc;
       }
-      set_scalars_kernel<<<1, 1, 0, st>>>(K(), tol, atol, maxiter, (unsigned long long)handle);
+      set_scalars_kernel<<<1, 1, 0, st>>>(K(), tol, atol, maxiter, (unsigned long long)handle,
+                                          hist, hist_len);
       GBPC_CUDA_TRY(cudaGetLastError());
       GBPC_CUDA_TRY(cudaGraphLaunch(exec, st));
     } else {
-      set_scalars_kernel<<<1, 1, 0, st>>>(K(), tol, atol, maxiter, 0ull);
+      set_scalars_kernel<<<1, 1, 0, st>>>(K(), tol, atol, maxiter, 0ull, hist, hist_len);
       if ((rc = record_init(b, x, st))) return rc;
       // Host-driven loop: chunks of iterations, then read the flag.
       int active = 1;
@@ -503,11 +508,22 @@ extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_gr
 extern "C" int gbpc_solver_run(gbpc_solver* h, const double* b, double* x, double tol, double atol,
                                int maxiter, int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
                                void* stream) {
+  NvtxRange nvtx_range("gbpc_solver_run");
   if (!h || !b || !x) {
     gbpc_set_error("gbpc_solver_run: bad arguments");
     return GBPC_ERR_ARG;
   }
   return h->s.run(b, x, tol, atol, maxiter, nit_dev, rr_dev, atol_sq_dev, (cudaStream_t)stream);
+}
+
+extern "C" int gbpc_solver_set_history(gbpc_solver* h, double* hist, int hist_len) {
+  if (!h || hist_len < 0 || (hist_len > 0 && !hist)) {
+    gbpc_set_error("gbpc_solver_set_history: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  h->s.hist = hist_len > 0 ? hist : nullptr;
+  h->s.hist_len = hist_len;
+  return GBPC_OK;
 }
 
 extern "C" int gbpc_solver_device_bytes(const gbpc_solver* h, size_t* bytes_host) {

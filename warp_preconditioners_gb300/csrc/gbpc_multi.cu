@@ -543,6 +543,7 @@ extern "C" int gbpc_msolver_create(gbpc_op* A, gbpc_op* M, int nseg, const int64
 extern "C" int gbpc_msolver_run(gbpc_msolver* h, const double* b, double* x, double tol,
                                 double atol, int maxiter, int32_t* nit_dev, double* rr_dev,
                                 double* atol_sq_dev, void* stream) {
+  NvtxRange nvtx_range("gbpc_msolver_run");
   if (!h || (h->s.n > 0 && (!b || !x))) {
     gbpc_set_error("gbpc_msolver_run: bad arguments");
     return GBPC_ERR_ARG;

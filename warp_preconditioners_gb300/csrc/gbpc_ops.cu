@@ -463,6 +463,7 @@ extern "C" int gbpc_op_fsai(int nrow, int block, const int32_t* g_off, const int
                             const void* g_val, const int32_t* gt_off, const int32_t* gt_col,
                             const void* gt_val, int value_dtype, int vector_dtype, void* stream,
                             gbpc_op** out) {
+  NvtxRange nvtx_range("gbpc_op_fsai");
   if (!out || nrow < 0 || !g_off || !gt_off || block < 1 || block > 4) {
     gbpc_set_error("gbpc_op_fsai: bad arguments");
     return GBPC_ERR_ARG;
@@ -546,6 +547,7 @@ extern "C" int gbpc_op_sqlap(int n, const int32_t* offsets, const int32_t* colum
                              const void* values, int dtype, const void* mass,
                              const int32_t* free_indices, int nfree, double mass_weight,
                              void* stream, gbpc_op** out) {
+  NvtxRange nvtx_range("gbpc_op_sqlap");
   if (!out || n < 0 || nfree < 0 || !offsets || (nfree > 0 && !free_indices) || (n > 0 && !mass)) {
     gbpc_set_error("gbpc_op_sqlap: bad arguments");
     return GBPC_ERR_ARG;
@@ -706,6 +708,7 @@ extern "C" int gbpc_op_block_jacobi(int nrow, int block, const int32_t* offsets,
                                     const int32_t* columns, const void* values, int dtype,
                                     double pivot_tolerance, void* inverse_out, void* stream,
                                     gbpc_op** out) {
+  NvtxRange nvtx_range("gbpc_op_block_jacobi");
   if (!out || nrow < 0 || block < 1 || block > 4 || (dtype != GBPC_F64 && dtype != GBPC_F32)) {
     gbpc_set_error("BlockJacobi requires square blocks of size 1 through 4");
     return GBPC_ERR_ARG;
@@ -788,6 +791,7 @@ extern "C" int gbpc_op_bilu0(int nrow, int block, const int32_t* offsets, const 
                              const void* values, int dtype, int factor_sweeps, int solve_sweeps,
                              double relaxation, double pivot_tolerance, void* factors_out,
                              void* inverse_out, void* stream, gbpc_op** out) {
+  NvtxRange nvtx_range("gbpc_op_bilu0");
   if (!out || nrow < 0 || block < 1 || block > 4 || (dtype != GBPC_F64 && dtype != GBPC_F32)) {
     gbpc_set_error("BlockILU0 requires square blocks of size 1 through 4");
     return GBPC_ERR_ARG;
@@ -859,6 +863,7 @@ extern "C" int gbpc_op_bilu0(int nrow, int block, const int32_t* offsets, const 
 
 extern "C" int gbpc_op_apply(gbpc_op* h, const void* x, const void* y, void* z, double alpha,
                              double beta, void* stream) {
+  NvtxRange nvtx_range("gbpc_op_apply");
   if (!h || !h->impl) {
     gbpc_set_error("gbpc_op_apply: null operator");
     return GBPC_ERR_ARG;

@@ -144,6 +144,7 @@ extern "C" int gbpc_spgemm(int nrow, int ncol, const int32_t* a_off, const int32
                            const int32_t* b_off, const int32_t* b_col, const double* b_val,
                            const double* add_diag, int32_t* c_off, int32_t* c_col, double* c_val,
                            int64_t* nnz_host, void* stream) {
+  NvtxRange nvtx_range("gbpc_spgemm");
   if (nrow < 0 || b_nrow < 0 || ncol < 0 || !c_off || !a_off || !b_off ||
       (add_diag && nrow > ncol)) {
     gbpc_set_error("gbpc_spgemm: bad arguments");

@@ -11,8 +11,10 @@ solve).
 
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import math
+import threading
 
 import torch
 
@@ -126,9 +128,19 @@ class Solver:
         """Device bytes of the Krylov state (work vectors and scalars)."""
         return _lib.object_bytes("gbpc_solver_device_bytes", self._h)
 
-    def run(self, b, x, tol=None, atol=None, maxiter=0):
+    def run(self, b, x, tol=None, atol=None, maxiter=0, history=None):
+        """Solve from the initial guess in x.  ``history`` (float64 device
+        tensor, optional) receives |r_k| for k < len(history), k = 0 the
+        initial residual; the iterates are the same with or without it."""
         tol = 1.0e-5 if tol is None else float(tol)
         atol = 0.0 if atol is None else float(atol)
+        if history is not None:
+            if history.dtype != torch.float64 or not history.is_cuda:
+                raise TypeError("history must be a float64 CUDA tensor")
+            _lib.call("gbpc_solver_set_history", self._h, _lib.ptr(_flat(history)),
+                      int(history.numel()))
+        else:
+            _lib.call("gbpc_solver_set_history", self._h, None, 0)
         _lib.call("gbpc_solver_run", self._h, _lib.ptr(_flat(b)), _lib.ptr(_flat(x)), tol, atol,
                   int(maxiter), _lib.ptr(self.nit), _lib.ptr(self.rr), _lib.ptr(self.atol_sq),
                   _lib.stream(self.A.device))
@@ -160,7 +172,7 @@ class _Vec:
         return self.out[:count].tolist()
 
 
-def _host_krylov(method, A, M, b, x, tol, atol, maxiter):
+def _host_krylov(method, A, M, b, x, tol, atol, maxiter, history=None):
     """CG / CR stepped from the host, for operators without a libgbpc handle
     (any ``LinearOperator(shape, dtype, device, matvec)``) and for float32
     systems.  Every vector update and dot product runs in libgbpc kernels on
@@ -201,6 +213,8 @@ def _host_krylov(method, A, M, b, x, tol, atol, maxiter):
         bb, rr, rz = v.read(3)
     atol_sq = max(atol, tol * math.sqrt(bb)) ** 2
     it = 0
+    if history is not None:
+        history.append(math.sqrt(max(rr, 0.0)))
     while rr > atol_sq and it < maxiter:
         if method == "cg":
             apply(A, p, Ap)
@@ -233,7 +247,39 @@ def _host_krylov(method, A, M, b, x, tol, atol, maxiter):
             v.axpby(1.0, z, beta, p, p)
             v.axpby(1.0, Az, beta, Ap, Ap)
         it += 1
+        if history is not None:
+            history.append(math.sqrt(max(rr, 0.0)))
     return it, rr, atol_sq
+
+
+_sampler = threading.local()
+
+
+@contextlib.contextmanager
+def sample_iterations(checkpoints, observe):
+    """Observe the residual norm of every cg / cr call inside the block at
+    iteration 0 and at each checkpoint (and where the solve stops early):
+    ``observe(i, |r_i|)``.  The solves run as they would without it -- same
+    iterates -- recording |r_k| in a device history buffer that is read
+    once the solve ends (the reference's benchmarks/residual_history.py
+    restarts Warp's loop at the checkpoints instead; trajectories are the
+    same either way)."""
+    points = sorted(set(int(i) for i in checkpoints if int(i) > 0))
+    prev = getattr(_sampler, "active", None)
+    _sampler.active = (points, observe)
+    try:
+        yield
+    finally:
+        _sampler.active = prev
+
+
+def _report(points, observe, hist, nit, maxiter):
+    observe(0, float(hist[0]))
+    for stop in sorted(set([p for p in points if p <= maxiter] + [int(maxiter)])):
+        if stop >= nit:
+            observe(nit, float(hist[nit]))
+            break
+        observe(stop, float(hist[stop]))
 
 
 def _cached_solver(method, A, M, use_cuda_graph) -> Solver:
@@ -267,8 +313,13 @@ def _solve(method, A, b, x, tol, atol, maxiter, M, callback, check_every, use_cu
     atol = 0.0 if atol is None else float(atol)
     native = (b.dtype == torch.float64 and getattr(A, "_op", None) is not None
               and (M is None or getattr(M, "_op", None) is not None))
+    sampler = getattr(_sampler, "active", None)
+    limit = int(maxiter) if int(maxiter) > 0 else b.numel()
     if not native:
-        it, rr, atol_sq = _host_krylov(method, A, M, b, x, tol, atol, int(maxiter))
+        hist = [] if sampler else None
+        it, rr, atol_sq = _host_krylov(method, A, M, b, x, tol, atol, int(maxiter), hist)
+        if sampler:
+            _report(sampler[0], sampler[1], hist, it, limit)
         if check_every == 0:
             dev = b.device
             return (torch.tensor([it], dtype=torch.int32, device=dev),
@@ -276,7 +327,10 @@ def _solve(method, A, b, x, tol, atol, maxiter, M, callback, check_every, use_cu
                     torch.tensor([atol_sq], dtype=torch.float64, device=dev))
         return it, math.sqrt(max(rr, 0.0)), math.sqrt(atol_sq)
     s = _cached_solver(method, A, M, use_cuda_graph)
-    nit, rr, atol_sq = s.run(b, x, tol, atol, maxiter)
+    hist = torch.empty(limit + 1, dtype=torch.float64, device=b.device) if sampler else None
+    nit, rr, atol_sq = s.run(b, x, tol, atol, maxiter, history=hist)
+    if sampler:
+        _report(sampler[0], sampler[1], hist.cpu().numpy(), int(nit.item()), limit)
     if check_every == 0:
         return nit.clone(), rr.clone(), atol_sq.clone()
     vals = torch.stack([nit.to(torch.float64), rr, atol_sq]).cpu()
