@@ -91,6 +91,9 @@ def parse_args():
     p.add_argument("--profile-iters", type=int, default=0,
                    help="profiling mode: one setup and one solve capped at this many "
                         "iterations, no timing (for ncu launch lists)")
+    p.add_argument("--profile-fsai", type=int, default=0,
+                   help="profiling mode: two FSAI setups of this width (and --step-size) "
+                        "on the --side system's Q, setup times only (for ncu)")
     return p.parse_args()
 
 
@@ -360,6 +363,17 @@ def main():
             rec.append((ev, its, pre))
         return pre
 
+    if args.profile_fsai > 0:
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pre = FSAI(Q, max_row_size=args.profile_fsai, max_step_size=args.step_size,
+                       kap_tolerance=1e-3)
+            torch.cuda.synchronize()
+            print(json.dumps({"profile_fsai": args.profile_fsai, "step": args.step_size, "n": n,
+                              "setup_ms": (time.perf_counter() - t0) * 1e3,
+                              "fsai_nnz": pre.G.nnz}), flush=True)
+        return
     if args.profile_iters > 0:
         op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
         pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
