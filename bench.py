@@ -75,6 +75,9 @@ def parse_args():
                    help="requests replayed from the seed-0 stream (its first N of 2,000)")
     p.add_argument("--c5-rate", type=float, default=4.0, help="Poisson arrivals per second")
     p.add_argument("--c5-slots", type=int, default=16)
+    p.add_argument("--c5-merge", type=int, default=0,
+                   help="also serve with queued requests of one system merged into batched "
+                        "solves of up to this many right-hand sides (0: skip that arm)")
     p.add_argument("--c5-budget-gb", type=float, default=120.0)
     p.add_argument("--c5-nmin", type=float, default=5e3)
     p.add_argument("--c5-nmax", type=float, default=5e5)
@@ -1295,6 +1298,17 @@ def run_c5(args, dev):
                "backward_error_max": max(a["berr"]) if a["berr"] else None}
         for kind, a in acc.items()}
 
+    if args.c5_merge:
+        mex = serve.GpuExecutor(cat, slots=args.c5_slots, tol=args.rtol, device=dev,
+                                merge_rhs=args.c5_merge)
+        msrv = serve.Server(mex, budget_bytes=budget)
+        t0 = time.perf_counter()
+        msrv.prepare(keys)
+        torch.cuda.synchronize()
+        out["served_merged_setup_s"] = time.perf_counter() - t0
+        out["served_merged"] = serve.summarize(msrv.run(stream, keep=lambda r: False))
+        out["served_merged_burst"] = serve.summarize(msrv.run(burst, keep=lambda r: False))
+        del msrv, mex
     if not args.c5_no_sequential:
         seq_ex = serve.GpuExecutor(cat, sequential=True, tol=args.rtol, device=dev)
         seq = serve.Server(seq_ex, budget_bytes=budget)
@@ -1305,6 +1319,11 @@ def run_c5(args, dev):
         sb, qb = out["served_burst"], out["sequential_burst"]
         out["speedup"] = {"capacity_solves_per_s": sb["solves_per_s"] / qb["solves_per_s"],
                           "p50": q["p50_ms"] / s["p50_ms"], "p99": q["p99_ms"] / s["p99_ms"]}
+        if args.c5_merge:
+            mb, m = out["served_merged_burst"], out["served_merged"]
+            out["speedup_merged"] = {
+                "capacity_solves_per_s": mb["solves_per_s"] / qb["solves_per_s"],
+                "p50": q["p50_ms"] / m["p50_ms"], "p99": q["p99_ms"] / m["p99_ms"]}
     kinds = collections.Counter(r.kind for r in stream)
     return {
         "metric": "serving p50/p99 latency (ms) and solves/s at 1e-8 relative residual",

@@ -102,3 +102,28 @@ def test_tight_budget_still_serves_everything(catalog):
     assert all(r.ok for r in out), [r.error for r in out if not r.ok]
     assert srv.stats["evictions"] > 0
     assert srv.peak <= srv.budget
+
+
+def test_merged_requests_match_alone_within_tolerance(catalog):
+    # Requests queued for one system are merged into one batched solve
+    # (merge_rhs): each keeps its own CG recurrence, so its x equals the
+    # unmerged solve to the solve tolerance (the fold of the batched dot
+    # products depends on the group's width, so not bit for bit).
+    keys = [("laplacian", 7), ("biharmonic", 5)]
+    for key in keys:
+        catalog.get(key)
+    stream = [serve.Request(i, *keys[i % 2], 1 + i % 3, 0.0, 1000 + i) for i in range(8)]
+    merged_ex = serve.GpuExecutor(catalog, slots=2, tol=TOL, merge_rhs=16)
+    merged = serve.Server(merged_ex).run(stream)
+    alone_ex = serve.GpuExecutor(catalog, slots=1, tol=TOL)
+    alone = serve.Server(alone_ex).run(stream)
+    for req, m, a in zip(stream, merged, alone):
+        assert m.ok and a.ok, (m.error, a.error)
+        x, xa = m.x.numpy(), a.x.numpy()
+        assert x.shape == xa.shape == (req.n, req.k)
+        assert np.abs(x - xa).max() <= 1e-6 * np.abs(xa).max(), req
+        assert all(abs(i - j) <= max(2, 0.03 * j) for i, j in zip(m.iterations, a.iterations))
+        A = host_matrix(catalog.get(req.key))
+        b = serve.request_rhs(req).numpy()
+        res = np.linalg.norm(b - A @ x, axis=0) / np.linalg.norm(b, axis=0)
+        assert res.max() < 50 * TOL, (req, res)

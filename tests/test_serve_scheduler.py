@@ -187,3 +187,47 @@ def test_estimate_bounds_host_sizes():
     assert e8 > serve.estimate_bytes(host, 2) > 0
     with pytest.raises(ValueError):
         serve.host_system("plate", 4)
+
+
+class MergingExecutor(FakeExecutor):
+    """FakeExecutor that also takes several queued requests of one system as
+    one solve (start_group / finish_group), like GpuExecutor(merge_rhs=...)."""
+
+    def __init__(self, merge_rhs, **kw):
+        super().__init__(**kw)
+        self.merge_rhs = merge_rhs
+        self.groups = []
+
+    def start_group(self, slot, handle, reqs, rhss):
+        assert len(reqs) == len(rhss) > 1
+        assert len({r.key for r in reqs}) == 1
+        assert sum(r.k for r in reqs) <= self.merge_rhs
+        self.groups.append([r.rid for r in reqs])
+        self.in_flight[reqs[0].key] = self.in_flight.get(reqs[0].key, 0) + 1
+        self.max_per_key = max(self.max_per_key, self.in_flight[reqs[0].key])
+        return [time.perf_counter() + self.duration, reqs, rhss]
+
+    def finish_group(self, token):
+        reqs, rhss = token[1], token[2]
+        self.in_flight[reqs[0].key] -= 1
+        return [(rhs, [7] * r.k) for r, rhs in zip(reqs, rhss)]
+
+
+def test_queued_requests_of_one_system_are_merged():
+    key_a, key_b = ("laplacian", 5), ("biharmonic", 4)
+    stream = [serve.Request(i, *(key_a if i % 3 else key_b), 2, 0.0, i) for i in range(12)]
+    ex = MergingExecutor(merge_rhs=6, slots=1, duration=0.002)
+    out = serve.Server(ex).run(stream, make_rhs=small_rhs)
+    assert all(r.ok for r in out)
+    # every request got its own right-hand sides back, in arrival order
+    for req, r in zip(stream, out):
+        assert float(r.x[0, 0]) == float(req.rid) and r.iterations == [7, 7]
+    assert ex.max_per_key == 1
+    merged = [g for g in ex.groups]
+    assert merged and all(len(g) <= 3 for g in merged)
+    # groups keep arrival order inside a system
+    for g in merged:
+        assert g == sorted(g)
+    # a merge never mixes systems and covers every request exactly once
+    started = [rid for _, _, rid in ex.started] + [rid for g in merged for rid in g]
+    assert sorted(started) == list(range(12))

@@ -19,6 +19,14 @@ vectors); requests for a busy system wait while others go ahead.  Results do
 not depend on what else runs: every kernel's reduction order is fixed by the
 system size and k, so a request gives bit-identical x alone and in the mix.
 
+``GpuExecutor(merge_rhs=m)`` also merges queued requests for one system:
+when a slot takes a request, later queued requests for the same system join
+it while their right-hand sides fit in m, and the group runs as one batched
+solve (each right-hand side its own CG recurrence, the matrices read once
+per iteration for all of them).  A merged request's x then equals its
+unmerged solve to the solve tolerance, not bit for bit (the batched dot
+products fold over the group's width).
+
 ``GpuExecutor(sequential=True)`` is the plain one-at-a-time float64 path for
 comparison: one slot, and the k right-hand sides of a request solved one
 after another with the single-vector solver.
@@ -297,21 +305,56 @@ class ResidentSystem:
             ev.record(stream)
         return ev
 
+    def launch_group(self, rhss, outs, nit_out: torch.Tensor, stream: torch.cuda.Stream,
+                     tol: float, maxiter: int):
+        """Several requests for this system as one batched solve: their
+        right-hand sides side by side in one [n, k] block (k = their sum <=
+        max_rhs), each column its own CG recurrence; x and the iteration
+        counts go back to each request's buffers."""
+        ks = [int(r.shape[1]) for r in rhss]
+        k = sum(ks)
+        if len(rhss) == 1 or k == 1 or self.bcg is None:
+            raise ValueError("launch_group takes two or more requests on a batched system")
+        if k > self.max_rhs or any(int(r.shape[0]) != self.n for r in rhss):
+            raise ValueError(f"request group of {k} right-hand sides does not fit system "
+                             f"{self.key} (n={self.n}, k <= {self.max_rhs})")
+        with torch.cuda.stream(stream):
+            B, X = self._blocks(k)
+            c = 0
+            for rhs, kk in zip(rhss, ks):
+                B[:, c:c + kk].copy_(rhs.to(B.device, non_blocking=True))
+                c += kk
+            X.zero_()
+            nit, _ = self.bcg.run(B, X, tol, 0.0, maxiter)
+            c = 0
+            for out, kk in zip(outs, ks):
+                out.copy_(X[:, c:c + kk], non_blocking=True)
+                c += kk
+            nit_out.copy_(nit[:k], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return ev
+
 
 class GpuExecutor:
     """Resident systems and slots (CUDA streams) on one GPU."""
 
     def __init__(self, catalog: Catalog, *, slots: int = 16, sequential: bool = False,
                  tol: float = 1e-8, maxiter: int = 0, width: int = 8, step: int = 1,
-                 kap: float = 1e-3, max_rhs: int = MAX_RHS, device="cuda"):
+                 kap: float = 1e-3, max_rhs: int = MAX_RHS, merge_rhs: int = 0, device="cuda"):
         if not torch.cuda.is_available():
             raise RuntimeError("GpuExecutor needs a CUDA device")
+        if merge_rhs and not 2 <= merge_rhs <= 32:
+            raise ValueError("merge_rhs must be 0 (off) or in [2, 32]")
         self.catalog = catalog
         self.sequential = sequential
         self.slots = 1 if sequential else int(slots)
         self.tol, self.maxiter = float(tol), int(maxiter)
         self.width, self.step, self.kap = width, step, kap
-        self.max_rhs = max_rhs
+        # Queued requests for one system are merged into batched solves of up
+        # to merge_rhs right-hand sides (0: one request per solve).
+        self.merge_rhs = 0 if sequential else int(merge_rhs)
+        self.max_rhs = max(max_rhs, self.merge_rhs)
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(self.slots)]
 
@@ -343,12 +386,28 @@ class GpuExecutor:
                            self.maxiter)
         return (ev, out, nit, rhs)
 
+    def start_group(self, slot: int, handle: ResidentSystem, reqs, rhss):
+        outs = [torch.empty((r.n, r.k), dtype=torch.float64, pin_memory=True) for r in reqs]
+        nit = torch.empty(sum(r.k for r in reqs), dtype=torch.int32, pin_memory=True)
+        ev = handle.launch_group(rhss, outs, nit, self.streams[slot], self.tol, self.maxiter)
+        return (ev, outs, nit, rhss, [r.k for r in reqs])
+
     def poll(self, token) -> bool:
         return token[0].query()
 
     def finish(self, token):
         token[0].synchronize()
         return token[1], [int(v) for v in token[2]]
+
+    def finish_group(self, token):
+        """(x, iterations) of each request of a group started by start_group."""
+        token[0].synchronize()
+        its = [int(v) for v in token[2]]
+        out, c = [], 0
+        for x, k in zip(token[1], token[4]):
+            out.append((x, its[c:c + k]))
+            c += k
+        return out
 
 
 # ---------------------------------------------------------------------------
@@ -464,16 +523,21 @@ class Server:
                 else:
                     pending.append((req, rhs))
             for entry in list(running):  # completions
-                slot, req, res, token = entry
+                slot, group, token = entry
                 if self.ex.poll(token):
-                    x, its = self.ex.finish(token)
-                    res.done = now()
-                    res.iterations = its
-                    res.x = x if keep is None or keep(req) else None
-                    results[req.rid] = res
+                    if len(group) == 1:
+                        outs = [self.ex.finish(token)]
+                    else:
+                        outs = self.ex.finish_group(token)
+                    t_done = now()
+                    for (req, res), (x, its) in zip(group, outs):
+                        res.done = t_done
+                        res.iterations = its
+                        res.x = x if keep is None or keep(req) else None
+                        results[req.rid] = res
                     running.remove(entry)
                     free_slots.append(slot)
-                    self.busy.discard(req.key)
+                    self.busy.discard(group[0][0].key)
                     progressed = True
             if free_slots and pending:  # dispatch, oldest first
                 for item in list(pending):
@@ -492,18 +556,37 @@ class Server:
                         continue
                     if handle is None:
                         continue
-                    pending.remove(item)
+                    group = [item]
+                    merge = int(getattr(self.ex, "merge_rhs", 0) or 0)
+                    if merge and req.k < merge:
+                        # Later queued requests for the same system join this
+                        # solve while the right-hand sides fit.
+                        total = req.k
+                        for other in pending:
+                            if other is not item and other[0].key == req.key \
+                                    and total + other[0].k <= merge:
+                                group.append(other)
+                                total += other[0].k
+                    for g in group:
+                        pending.remove(g)
                     slot = free_slots.pop()
-                    res = Result(req.rid, req.key, req.k, req.arrival, start=now())
+                    t_start = now()
+                    members = [(g[0], Result(g[0].rid, g[0].key, g[0].k, g[0].arrival,
+                                             start=t_start)) for g in group]
                     try:
-                        token = self.ex.start(slot, handle, req, rhs)
+                        if len(group) == 1:
+                            token = self.ex.start(slot, handle, req, rhs)
+                        else:
+                            token = self.ex.start_group(slot, handle, [g[0] for g in group],
+                                                        [g[1] for g in group])
                     except (ValueError, RuntimeError) as e:
                         free_slots.append(slot)
-                        fail(req, f"launch failed: {e}")
+                        for g in group:
+                            fail(g[0], f"launch failed: {e}")
                         progressed = True
                         continue
                     self.busy.add(req.key)
-                    running.append((slot, req, res, token))
+                    running.append((slot, members, token))
                     progressed = True
             if (not prod.is_alive() and inbox.empty() and not pending and not running
                     and len(results) < expected):
