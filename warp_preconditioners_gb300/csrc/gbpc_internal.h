@@ -178,6 +178,22 @@ struct Operator {
                     const int* guard, const DotSpec* dot, cudaStream_t st) = 0;
   // True when x may not alias z in apply (the generic entry copies x first).
   virtual bool gathers_x() const { return true; }
+  // The scalar float64 sliced-ELL matrices whose products in this order
+  // are the whole apply (z = M_k ... M_1 x, no epilogue), or 0 when the
+  // operator is not of that form.  Lets a solver run them itself.
+  virtual int scalar_products(const Sell** out, int max) const {
+    (void)out;
+    (void)max;
+    return 0;
+  }
+  // The factored squared Laplacian with every vertex free, float64: its L,
+  // 1/m and w m (apply = L((1/m) o (L x)) + (w m) o x), or false.
+  virtual bool factored_parts(const Sell** L, const void** inv_mass, const void** wmass) const {
+    (void)L;
+    (void)inv_mass;
+    (void)wmass;
+    return false;
+  }
   DevBuf alias_scratch;  // copy of x when x aliases z
 };
 

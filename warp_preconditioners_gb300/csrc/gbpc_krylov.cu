@@ -18,7 +18,11 @@
 //                       Az = A z  [+ z.Az -> beta, it++, continue?]
 //                       p = z + beta p, Ap = Az + beta Ap
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
+#include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "gbpc_common.cuh"
@@ -158,6 +162,311 @@ int vec_grid(int64_t n) { return std::min<int64_t>(grid_for(n, kThreads), kSms *
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Small systems: the whole PCG solve as one cooperative kernel.
+//
+// Below a few tens of thousands of rows an iteration of the graph loop is a
+// handful of tiny kernels, each paying its launch and drain (~28 us per
+// iteration on the 64 x 64 Laplacian against ~2 us of arithmetic).  For a
+// scalar sparse operator and an FSAI (or no) preconditioner, one
+// cooperative launch runs every iteration instead: the grid syncs between
+// the dependent phases (5 per iteration), every CTA adds the per-CTA
+// partial sums of a dot product in the same order (so every CTA holds the
+// same alpha, beta and stopping decision), and the loop ends at the same
+// test as the graph loop (r.r <= max(atol, tol |b|)^2 or maxiter).  Rows
+// sum their entries in storage order, as in the sliced-ELL kernels.
+
+namespace coop {
+
+namespace cgr = cooperative_groups;
+
+constexpr int kThreadsC = 256;  // 8 warps per CTA
+constexpr int kMaxRows = 65536;
+// Up to this many rows the solve runs on one thread-block cluster (16 CTAs,
+// or 8 where 16 cannot be scheduled): hardware cluster barriers and sums
+// exchanged through distributed shared memory.  Larger systems use a
+// cooperative grid of up to one CTA slot per resident CTA.
+constexpr int kClusterRows = 32768;
+
+struct Mat {
+  int nrow, nslices;
+  const int64_t* slice_ptr;
+  const int32_t* cols;
+  const double* vals;
+  const int32_t* perm;
+};
+
+struct Args {
+  Mat A, G, GT;  // G.nslices < 0: no preconditioner
+  // inv_mass != nullptr: A is the factored squared Laplacian with every
+  // vertex free, A x = L ((1/m) o (L x)) + (w m) o x with L = A above.
+  const double* inv_mass;
+  const double* wmass;
+  int64_t n;
+  const double* b;
+  double* x;
+  double *r, *z, *p, *Ap, *t, *u;
+  double* partials;  // [2][gridDim.x]
+  KrylovScalars* ks;
+};
+
+// Row epilogues of `product`, those of the sliced-ELL kernels: plain,
+// (1/m) o acc, acc + (w m) o x.
+enum CoopEpi : int { CE_PLAIN = 0, CE_SCALE = 1, CE_MASS = 2 };
+
+// z = m x (one warp per slice, rows in storage order); dot_part += z . w.
+__device__ __forceinline__ void product(const Mat& m, const double* x, double* z, const double* w,
+                                        double& dot_part, int epi = CE_PLAIN,
+                                        const double* aux0 = nullptr,
+                                        const double* aux1 = nullptr) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (kThreadsC / 32);
+  for (int s = blockIdx.x * (kThreadsC / 32) + (threadIdx.x >> 5); s < m.nslices; s += nwarps) {
+    const int64_t base = m.slice_ptr[s];
+    const int width = (int)((m.slice_ptr[s + 1] - base) / kSlice);
+    double acc = 0.0;
+    // Chunks of 8 entries: all column and value loads, then all x gathers,
+    // then the multiply-adds in entry order (one dependent round trip per
+    // chunk instead of two per entry).
+    for (int k0 = 0; k0 < width; k0 += 8) {
+      int c[8];
+      double v[8], xv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int64_t e = base + (int64_t)(k0 + j) * kSlice + lane;
+        const bool in = k0 + j < width;
+        c[j] = in ? m.cols[e] : -1;
+        v[j] = in ? m.vals[e] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) xv[j] = c[j] >= 0 ? x[c[j]] : 0.0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (c[j] >= 0) acc = fma(v[j], xv[j], acc);
+    }
+    const int row = s * kSlice + lane;
+    if (row < m.nrow) {
+      const int orow = m.perm ? m.perm[row] : row;
+      double out = acc;
+      if (epi == CE_SCALE) out = aux0[orow] * acc;
+      else if (epi == CE_MASS) out = fma(aux0[orow], aux1[orow], acc);
+      z[orow] = out;
+      if (w) dot_part = fma(out, w[orow], dot_part);
+    }
+  }
+}
+
+// CTA sum of one value per thread, in thread 0 (fixed order).
+__device__ __forceinline__ double cta_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double c = 0.0;
+  if (threadIdx.x == 0)
+    for (int w2 = 0; w2 < kThreadsC / 32; ++w2) c += sh[w2];
+  return c;
+}
+
+// Synchronisation and the exchange of per-CTA sums, two ways.  Both return
+// the same total on every CTA: the CTA sums added in CTA order (lanes take
+// them strided, then a fixed butterfly).  Two slots alternate, so a CTA
+// that runs ahead never overwrites sums another CTA is still reading.
+//
+// GridSync: any grid of co-resident CTAs (cooperative launch); the sums
+// go through global memory and grid syncs.
+struct GridSync {
+  cgr::grid_group g;
+  double* partials;  // [2][gridDim.x]
+  __device__ explicit GridSync(double* p) : g(cgr::this_grid()), partials(p) {}
+  __device__ void sync() { g.sync(); }
+  __device__ double total(double v, int slot, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double c = cta_sum(v, sh);
+    if (threadIdx.x == 0) partials[(size_t)slot * gridDim.x + blockIdx.x] = c;
+    g.sync();
+    if (warp == 0) {
+      double a = 0.0;
+      for (unsigned int q = lane; q < gridDim.x; q += 32)
+        a += __ldcg(partials + (size_t)slot * gridDim.x + q);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) sh[kThreadsC / 32] = a;
+    }
+    __syncthreads();
+    const double t = sh[kThreadsC / 32];
+    __syncthreads();
+    return t;
+  }
+  __device__ void finish() {}
+};
+
+// ClusterSync: the grid is one thread-block cluster; syncs are the
+// cluster's hardware barrier and every CTA reads the others' sums from
+// their shared memory (distributed shared memory), no global round trip.
+struct ClusterSync {
+  cgr::cluster_group c;
+  double* xch;  // this CTA's shared [2] exchange slots
+  __device__ ClusterSync(double* x) : c(cgr::this_cluster()), xch(x) {}
+  __device__ void sync() { c.sync(); }
+  __device__ double total(double v, int slot, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double cs = cta_sum(v, sh);
+    if (threadIdx.x == 0) xch[slot] = cs;
+    c.sync();
+    if (warp == 0) {
+      const unsigned int ranks = c.num_blocks();
+      double a = 0.0;
+      for (unsigned int q = lane; q < ranks; q += 32) a += *c.map_shared_rank(xch + slot, q);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) sh[kThreadsC / 32] = a;
+    }
+    __syncthreads();
+    const double t = sh[kThreadsC / 32];
+    __syncthreads();
+    return t;
+  }
+  // No CTA leaves while another may still read its shared memory.
+  __device__ void finish() { c.sync(); }
+};
+
+// Ap = A x with dot_part += Ap . w: one product, or the factored squared
+// Laplacian's two with a sync between them.
+template <class S>
+__device__ __forceinline__ void apply_a(S& grid, const Args& a, const double* x, double* out,
+                                        const double* w, double& dot_part) {
+  if (a.inv_mass) {
+    double d0 = 0.0;
+    product(a.A, x, a.u, nullptr, d0, CE_SCALE, a.inv_mass);
+    grid.sync();
+    product(a.A, a.u, out, w, dot_part, CE_MASS, a.wmass, x);
+  } else {
+    product(a.A, x, out, w, dot_part);
+  }
+}
+
+// z = M r (G then G^T, a sync between them; or z = r); returns this
+// thread's share of r.z.
+template <class S>
+__device__ __forceinline__ double precondition(S& grid, const Args& a, bool precond, int64_t gt,
+                                               int64_t gs) {
+  double prz = 0.0;
+  if (precond) {
+    double d0 = 0.0;
+    product(a.G, a.r, a.t, nullptr, d0);
+    grid.sync();
+    product(a.GT, a.t, a.z, a.r, prz);
+  } else {
+    for (int64_t i = gt; i < a.n; i += gs) {
+      const double ri = a.r[i];
+      a.z[i] = ri;
+      prz = fma(ri, ri, prz);
+    }
+  }
+  return prz;
+}
+
+template <class S>
+__global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
+  __shared__ double sh[kThreadsC / 32 + 1];
+  __shared__ double xch[2];
+  S grid = [&]() {
+    if constexpr (std::is_same<S, ClusterSync>::value) return S(xch);
+    else return S(a.partials);
+  }();
+  KrylovScalars* ks = a.ks;
+  const int64_t n = a.n;
+  const int64_t gt = (int64_t)blockIdx.x * kThreadsC + threadIdx.x;
+  const int64_t gs = (int64_t)gridDim.x * kThreadsC;
+  const bool precond = a.G.nslices >= 0;
+  int slot = 0;
+  const double tol = ks->tol, atol = ks->atol;
+  const int maxiter = ks->maxiter;
+  double* hist = ks->hist;
+  const int hist_len = ks->hist_len;
+  // r = b - A x; b.b and r.r.
+  double dummy = 0.0;
+  apply_a(grid, a, a.x, a.Ap, nullptr, dummy);
+  grid.sync();
+  double pbb = 0.0, prr = 0.0;
+  for (int64_t i = gt; i < n; i += gs) {
+    const double bi = a.b[i];
+    const double ri = bi - a.Ap[i];
+    a.r[i] = ri;
+    pbb = fma(bi, bi, pbb);
+    prr = fma(ri, ri, prr);
+  }
+  const double bb = grid.total(pbb, slot, sh);
+  slot ^= 1;
+  double rr = grid.total(prr, slot, sh);
+  slot ^= 1;
+  const double at = fmax(atol, tol * sqrt(bb));
+  const double atol_sq = at * at;
+  if (gt == 0 && hist && hist_len > 0) hist[0] = sqrt(rr);
+  // z = M r, rz = r.z, p = z.
+  double prz = precondition(grid, a, precond, gt, gs);
+  double rz = grid.total(prz, slot, sh);
+  slot ^= 1;
+  for (int64_t i = gt; i < n; i += gs) a.p[i] = a.z[i];
+  grid.sync();
+  int it = 0;
+  double alpha = 0.0, beta = 0.0, pap = 0.0;
+  while (rr > atol_sq && it < maxiter) {
+    double ppap = 0.0;
+    apply_a(grid, a, a.p, a.Ap, a.p, ppap);
+    pap = grid.total(ppap, slot, sh);
+    slot ^= 1;
+    alpha = rz / pap;
+    double prr2 = 0.0;
+    for (int64_t i = gt; i < n; i += gs) {
+      a.x[i] = fma(alpha, a.p[i], a.x[i]);
+      const double ri = fma(-alpha, a.Ap[i], a.r[i]);
+      a.r[i] = ri;
+      prr2 = fma(ri, ri, prr2);
+    }
+    rr = grid.total(prr2, slot, sh);
+    slot ^= 1;
+    if (gt == 0 && hist && it + 1 < hist_len) hist[it + 1] = sqrt(rr);
+    const double prz2 = precondition(grid, a, precond, gt, gs);
+    const double rz_new = grid.total(prz2, slot, sh);
+    slot ^= 1;
+    beta = rz_new / rz;
+    rz = rz_new;
+    ++it;
+    for (int64_t i = gt; i < n; i += gs) a.p[i] = fma(beta, a.p[i], a.z[i]);
+    grid.sync();
+  }
+  grid.finish();
+  if (gt == 0) {
+    ks->bb = bb;
+    ks->atol_sq = atol_sq;
+    ks->rr = rr;
+    ks->rz = rz;
+    ks->denom = pap;
+    ks->alpha = alpha;
+    ks->beta = beta;
+    ks->it = it;
+    ks->active = 0;
+  }
+}
+
+Mat mat_of(const Sell& m) {
+  return Mat{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
+             m.vals.as<double>(), m.perm.p ? m.perm.as<int32_t>() : nullptr};
+}
+
+bool enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBPC_COOP");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+}  // namespace coop
+
 struct Solver {
   size_t device_bytes = 0;  // DevBuf bytes held (declared first: released last)
   int method = GBPC_CG;
@@ -174,7 +483,13 @@ struct Solver {
   double* hist = nullptr;  // residual history of the next runs (gbpc_solver_set_history)
   int hist_len = 0;
   bool use_pdl = true;  // programmatic dependent launches inside the loop body
-  DevBuf r, z, p, Ap, Az, y, ks, zeros;
+  // Small scalar systems (coop::kMaxRows) with a sparse operator and an
+  // FSAI or no preconditioner run as one cooperative kernel (coop_grid CTAs).
+  bool coop = false;
+  int coop_grid = 0;
+  int coop_cluster = 0;  // > 0: the grid is one cluster of this many CTAs
+  coop::Args cargs{};
+  DevBuf r, z, p, Ap, Az, y, ks, zeros, t, u, cpart;
   ReduceBuf rb;
   // Cached graph for the last (b, x) pair.
   cudaGraphExec_t exec = nullptr;
@@ -391,11 +706,117 @@ struct Solver {
     return GBPC_OK;
   }
 
+  // Decide whether this solver runs as one cooperative kernel (small
+  // scalar CG with a sparse operator and an FSAI or no preconditioner, the
+  // graph loop requested) and size its grid: enough CTAs for one slice per
+  // warp, at most what can be resident at once.
+  int setup_coop() {
+    coop = false;
+    if (!coop::enabled() || method != GBPC_CG || !use_graph || low || n > coop::kMaxRows ||
+        n < 1)
+      return GBPC_OK;
+    const Sell* pa[1] = {nullptr};
+    const Sell* pm[2] = {nullptr, nullptr};
+    const void* inv_mass = nullptr;
+    const void* wmass = nullptr;
+    if (A->scalar_products(pa, 1) != 1 && !A->factored_parts(pa, &inv_mass, &wmass))
+      return GBPC_OK;
+    if (M && M->scalar_products(pm, 2) != 2) return GBPC_OK;
+    int dev = 0, sms = 0, per_sm = 0;
+    GBPC_CUDA_TRY(cudaGetDevice(&dev));
+    GBPC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GBPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, coop::pcg_kernel<coop::GridSync>, coop::kThreadsC, 0));
+    int coop_ok = 0;
+    GBPC_CUDA_TRY(cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop_ok || per_sm < 1) return GBPC_OK;
+    const int warps = coop::kThreadsC / 32;
+    int need = (pa[0]->nslices + warps - 1) / warps;
+    if (M) need = std::max(need, std::max((pm[0]->nslices + warps - 1) / warps,
+                                          (pm[1]->nslices + warps - 1) / warps));
+    coop_grid = std::max(1, std::min(need, sms * per_sm));
+    coop_cluster = 0;
+    if (n <= coop::kClusterRows) {
+      auto kern = coop::pcg_kernel<coop::ClusterSync>;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+          cudaSuccess)
+        cudaGetLastError();
+      for (int c : {16, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(c);
+        cfg.blockDim = dim3(coop::kThreadsC);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = c;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) == cudaSuccess && clusters > 0) {
+          coop_cluster = c;
+          break;
+        }
+        cudaGetLastError();
+      }
+    }
+    int rc;
+    if ((rc = t.alloc(sizeof(double) * n))) return rc;
+    if (inv_mass && (rc = u.alloc(sizeof(double) * n))) return rc;
+    if ((rc = cpart.alloc(sizeof(double) * 2 * coop_grid))) return rc;
+    cargs = coop::Args{};
+    cargs.A = coop::mat_of(*pa[0]);
+    cargs.inv_mass = (const double*)inv_mass;
+    cargs.wmass = (const double*)wmass;
+    cargs.u = inv_mass ? u.as<double>() : nullptr;
+    if (M) {
+      cargs.G = coop::mat_of(*pm[0]);
+      cargs.GT = coop::mat_of(*pm[1]);
+    } else {
+      cargs.G.nslices = -1;
+      cargs.GT.nslices = -1;
+    }
+    cargs.n = n;
+    cargs.r = r.as<double>();
+    cargs.z = z.as<double>();
+    cargs.p = p.as<double>();
+    cargs.Ap = Ap.as<double>();
+    cargs.t = t.as<double>();
+    cargs.partials = cpart.as<double>();
+    cargs.ks = K();
+    coop = true;
+    return GBPC_OK;
+  }
+
   int run(const double* b, double* x, double tol, double atol, int maxiter, int32_t* nit_dev,
           double* rr_dev, double* atol_sq_dev, cudaStream_t st) {
     if (maxiter <= 0) maxiter = (int)std::min<int64_t>(n, 0x7fffffff);
     int rc;
-    if (use_graph) {
+    if (coop) {
+      set_scalars_kernel<<<1, 1, 0, st>>>(K(), tol, atol, maxiter, 0ull, hist, hist_len);
+      GBPC_CUDA_TRY(cudaGetLastError());
+      coop::Args a = cargs;
+      a.b = b;
+      a.x = x;
+      if (coop_cluster > 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(coop_cluster);
+        cfg.blockDim = dim3(coop::kThreadsC);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = coop_cluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        GBPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, coop::pcg_kernel<coop::ClusterSync>, a));
+      } else {
+        void* params[] = {&a};
+        GBPC_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)coop::pcg_kernel<coop::GridSync>,
+                                                  coop_grid, coop::kThreadsC, params, 0, st));
+      }
+    } else if (use_graph) {
       if (!exec || last_b != b || last_x != x) {
         rc = build_graph(b, x, st);
         if (rc && use_pdl) {  // capture without programmatic launches instead
@@ -497,6 +918,7 @@ extern "C" int gbpc_solver_create(int method, gbpc_op* A, gbpc_op* M, int use_gr
   if (!rc) rc = s.rb.init((cudaStream_t)stream);
   if (!rc && cudaMemsetAsync(s.ks.p, 0, sizeof(KrylovScalars), (cudaStream_t)stream) != cudaSuccess)
     rc = GBPC_ERR_CUDA;
+  if (!rc) rc = s.setup_coop();
   if (rc) {
     delete h;
     return rc;

@@ -227,6 +227,11 @@ struct SparseOp : Operator {
             const DotSpec* dot, cudaStream_t st) override {
     return sell_spmv(m, vdtype, x, y, z, alpha, beta, guard, EpiHost{}, dot, st);
   }
+  int scalar_products(const Sell** out, int max) const override {
+    if (max < 1 || m.B != 1 || m.vdtype != GBPC_F64 || vdtype != GBPC_F64) return 0;
+    out[0] = &m;
+    return 1;
+  }
 };
 
 struct FsaiOp : Operator {
@@ -243,6 +248,14 @@ struct FsaiOp : Operator {
     return sell_spmv(gt, vdtype, tmp.p, y, z, alpha, beta, guard, EpiHost{}, dot, st);
   }
   bool gathers_x() const override { return false; }
+  int scalar_products(const Sell** out, int max) const override {
+    if (max < 2 || g.B != 1 || g.vdtype != GBPC_F64 || gt.vdtype != GBPC_F64 ||
+        vdtype != GBPC_F64)
+      return 0;
+    out[0] = &g;
+    out[1] = &gt;
+    return 2;
+  }
 };
 
 struct SqlapOp : Operator {
@@ -280,6 +293,13 @@ struct SqlapOp : Operator {
     return sell_spmv(bwd, vdtype, tmp.p, y, z, alpha, beta, guard, b, dot, st);
   }
   bool gathers_x() const override { return false; }
+  bool factored_parts(const Sell** L, const void** im, const void** wm) const override {
+    if (!identity_free || vdtype != GBPC_F64 || bwd.B != 1 || bwd.vdtype != GBPC_F64) return false;
+    *L = &bwd;
+    *im = inv_mass.p;
+    *wm = wmass.p;
+    return true;
+  }
   int rhs(const void* u, void* out, cudaStream_t st) {
     int rc = sell_spmv(bnd, vdtype, u, nullptr, tmp.p, 1.0, 0.0, nullptr, EpiHost{}, nullptr, st);
     if (rc) return rc;
