@@ -478,6 +478,7 @@ def main():
                                                         ms_per_step)
     if not args.no_mixed:
         line["multi_system"] = measure_multi_system(dev)
+        line["multi_system_small"] = measure_multi_system(dev, sides=(17, 18, 19, 20) * 8)
     line["refit"] = measure_refit(args, prob, Q, dev)
     line["assembly"] = measure_assembly(prob, dev)
     if args.lifted:
@@ -795,13 +796,14 @@ def measure_refit(args, prob, Q, dev):
 
 
 def measure_multi_system(dev, sides=tuple(range(17, 38, 2)) + (18, 24, 30, 36, 22), tol=1e-8):
-    """Many independent smoothing systems of uneven size in one solve
-    (multi.MultiSystemSolver: block-diagonal operator and FSAI, per-system
-    scalars and stopping tests) against the same systems solved one at a
-    time with the drop-in float64 solver.  Tet cubes of the given sides
-    (4,913 to 50,653 unknowns), FSAI w8, first right-hand side, CG to `tol`;
-    operators and factors built beforehand, solve time only, CUDA-event
-    medians of 3."""
+    """Many independent smoothing systems of uneven size in one launch, two
+    ways -- multi.MultiSystemSolver (block-diagonal operator and FSAI,
+    per-system scalars and stopping tests, every product over all systems)
+    and multi.ClusterSolver (one thread-block cluster per system, each with
+    its own operators) -- against the same systems solved one at a time
+    with the drop-in float64 solver.  Tet cubes of the given sides, FSAI
+    w8, first right-hand side, CG to `tol`; operators and factors built
+    beforehand, solve time only, CUDA-event medians of 3."""
     import torch
 
     from warp_preconditioners_gb300 import FSAI, SquaredLaplacianOperator, from_scipy, linear, problems
@@ -836,11 +838,11 @@ def measure_multi_system(dev, sides=tuple(range(17, 38, 2)) + (18, 24, 30, 36, 2
                                       mass_weight=ALPHA)
         solver = linear.Solver("cg", op, FSAI(Q, max_row_size=8))
         x = torch.zeros(n, dtype=torch.float64, device=dev)
-        solo.append((solver, b, x))
+        solo.append((op, solver, b, x))
 
     def run_solo():
         its = []
-        for solver, b, x in solo:
+        for _, solver, b, x in solo:
             x.zero_()
             nit, _, _ = solver.run(b, x, tol=tol, maxiter=100000)
             its.append(nit)
@@ -865,8 +867,25 @@ def measure_multi_system(dev, sides=tuple(range(17, 38, 2)) + (18, 24, 30, 36, 2
 
     run_multi()
     t_multi, its_multi = timed(run_multi)
+    # The same systems each on its own thread-block cluster, one launch, no
+    # concatenation (multi.ClusterSolver).
+    from warp_preconditioners_gb300.multi import ClusterSolver
+
+    csolver = ClusterSolver([(s[0], s[1].M) for s in solo])
+    cbs = [s[2] for s in solo]
+    cxs = [torch.zeros_like(b) for b in cbs]
+
+    def run_cluster():
+        for x in cxs:
+            x.zero_()
+        nit, _, _ = csolver.run(cbs, cxs, tol=tol, maxiter=100000)
+        return nit
+
+    run_cluster()
+    t_cluster, its_cluster = timed(run_cluster)
     its_solo = [int(i.item()) for i in its_solo]
     its_multi = [int(i) for i in its_multi.cpu().tolist()]
+    its_cluster = [int(i) for i in its_cluster.cpu().tolist()]
     S = len(sizes)
     return {"workload": (f"{S} biharmonic smoothing systems on tet cubes of sides "
                          f"{min(sides)}..{max(sides)} ({min(sizes)}..{max(sizes)} unknowns, "
@@ -874,7 +893,11 @@ def measure_multi_system(dev, sides=tuple(range(17, 38, 2)) + (18, 24, 30, 36, 2
             "one_at_a_time_ms": t_solo, "one_launch_ms": t_multi,
             "one_at_a_time_solves_per_s": S * 1e3 / t_solo,
             "one_launch_solves_per_s": S * 1e3 / t_multi, "speedup": t_solo / t_multi,
-            "iterations_one_at_a_time": its_solo, "iterations_one_launch": its_multi}
+            "cluster_per_system_ms": t_cluster,
+            "cluster_per_system_solves_per_s": S * 1e3 / t_cluster,
+            "cluster_speedup": t_solo / t_cluster,
+            "iterations_one_at_a_time": its_solo, "iterations_one_launch": its_multi,
+            "iterations_cluster_per_system": its_cluster}
 
 
 def measure_batched_rhs4(args, prob, Q, K, mass, dev, ms_per_step):

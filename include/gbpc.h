@@ -459,6 +459,27 @@ int gbpc_msolver_run(gbpc_msolver* solver, const double* b, double* x, double to
 int gbpc_msolver_device_bytes(const gbpc_msolver* solver, size_t* bytes_host);
 int gbpc_msolver_destroy(gbpc_msolver* solver);
 
+/* Many independent small systems in one launch, each solved by its own
+ * thread-block cluster of 16 CTAs (8 where 16 cannot be scheduled): system s
+ * is A[s] (a float64 scalar sparse operator, or a factored squared
+ * Laplacian with every vertex free) preconditioned by M[s] (a float64
+ * scalar FSAI, or NULL).  Nothing is concatenated; each cluster stops when
+ * its own system passes the stopping test (r.r <= max(atol, tol |b_s|)^2,
+ * or maxiter; maxiter <= 0 means the system's size).  b_host / x_host are
+ * host arrays of nsys device pointers; nit_dev / rr_dev / atol_sq_dev hold
+ * nsys entries (any may be NULL).  A system's iterates equal those of the
+ * single-system cluster kernel that gbpc_solver uses for CG below 32,768
+ * rows.  Stream-ordered.  No reference counterpart. */
+typedef struct gbpc_csolver gbpc_csolver;
+int gbpc_csolver_create(int nsys, gbpc_op* const* A, gbpc_op* const* M, void* stream,
+                        gbpc_csolver** out);
+int gbpc_csolver_run(gbpc_csolver* solver, const double* const* b_host, double* const* x_host,
+                     double tol, double atol, int maxiter, int32_t* nit_dev, double* rr_dev,
+                     double* atol_sq_dev, void* stream);
+int gbpc_csolver_cluster_size(const gbpc_csolver* solver, int* cluster_host);
+int gbpc_csolver_device_bytes(const gbpc_csolver* solver, size_t* bytes_host);
+int gbpc_csolver_destroy(gbpc_csolver* solver);
+
 /* ------------------------------------------------------------------------ */
 /* Vector utilities (dtype GBPC_F64 or GBPC_F32; stream-ordered, no
  * allocation, no synchronisation).                                          */

@@ -1,9 +1,11 @@
-"""Small systems solved by one cooperative kernel (the graph loop's
-replacement below 65,536 rows for a scalar sparse operator with an FSAI or
-no preconditioner): the same method and stopping rule as the graph loop of
-separate kernels (`use_cuda_graph=False` runs those), so iteration counts
-agree to rounding and both reach the oracle's PCG; repeated runs give the
-same bits; maxiter and a converged start behave like CG."""
+"""Small systems solved by one kernel on one thread-block cluster (the
+graph loop's replacement when a CG iteration needs at most ~600k
+multiply-adds, for a scalar sparse or factored squared-Laplacian operator
+with an FSAI or no preconditioner; larger systems, here the 40^3 ones, keep
+the graph loop): the same method and stopping rule as the loop of separate
+kernels (`use_cuda_graph=False` runs those), so iteration counts agree to
+rounding and both reach the oracle's PCG; repeated runs give the same bits;
+maxiter and a converged start behave like CG."""
 
 import numpy as np
 import pytest

@@ -130,3 +130,57 @@ def test_converged_and_capped_systems_stop_alone(systems):
         from warp_preconditioners_gb300.multi import MultiSystemSolver
 
         MultiSystemSolver(solver.A, solver.M, sizes[:-1])
+
+
+def test_cluster_solver_matches_each_system_alone(oracle, systems):
+    # One launch, one thread-block cluster per system, each system with its
+    # own operators: biharmonic factored operators with FSAI, a Laplacian
+    # with FSAI, a Laplacian with no preconditioner, and a zero right-hand
+    # side.  Each system's x and iteration count equal the drop-in solver's
+    # on that system alone (the same cluster kernel below 32,768 rows).
+    from warp_preconditioners_gb300 import (FSAI, SparseOperator, SquaredLaplacianOperator,
+                                            from_scipy, linear, problems)
+    from warp_preconditioners_gb300.multi import ClusterSolver
+
+    dev = cuda()
+    pairs, rhs, mats = [], [], []
+    for K, mass, Q, b in systems:
+        n = K.shape[0]
+        op = SquaredLaplacianOperator(from_scipy(K, dev), vec(mass),
+                                      torch.arange(n, dtype=torch.int32, device=dev),
+                                      mass_weight=ALPHA)
+        pairs.append((op, FSAI(from_scipy(Q, dev), max_row_size=8)))
+        rhs.append(b)
+        mats.append(Q)
+    for side, pre in ((40, True), (30, False)):
+        a = problems.laplacian_2d(side)
+        A = from_scipy(a, dev)
+        pairs.append((SparseOperator(A), FSAI(A, max_row_size=8) if pre else None))
+        rhs.append(problems.uniform_rhs(a.shape[0], side))
+        mats.append(a)
+    rhs[1] = np.zeros_like(rhs[1])
+    solver = ClusterSolver(pairs)
+    assert solver.cluster_size in (8, 16)
+    bs = [vec(b) for b in rhs]
+    xs = [torch.zeros_like(b) for b in bs]
+    nit, rr, atol_sq = solver.run(bs, xs, tol=1e-8, maxiter=20000)
+    nit = nit.cpu().numpy()
+    assert nit[1] == 0 and torch.count_nonzero(xs[1]) == 0
+    assert (rr <= atol_sq).all()
+    for s, ((A, M), b, x) in enumerate(zip(pairs, bs, xs)):
+        alone = torch.zeros_like(b)
+        it, _, _ = linear.Solver("cg", A, M).run(b, alone, tol=1e-8, maxiter=20000)
+        assert int(it.item()) == int(nit[s]), s
+        assert torch.equal(alone, x), s
+    # a second run gives the same bits
+    xs2 = [torch.zeros_like(b) for b in bs]
+    solver.run(bs, xs2, tol=1e-8, maxiter=20000)
+    assert all(torch.equal(a, b) for a, b in zip(xs, xs2))
+    # against the oracle's PCG on the first biharmonic system
+    K, mass, Q, b0 = systems[0]
+    qc = oracle.CSR(Q.indptr, Q.indices, Q.data)
+    g, gt, _ = oracle.fsai(qc, width=8)
+    kc = oracle.CSR(K.indptr, K.indices, K.data)
+    _, it_or, _, _ = oracle.krylov("cg", oracle.Operator.sqlap(kc, mass, ALPHA), b0,
+                                   M=oracle.Operator.fsai(g, gt), tol=1e-8, maxiter=20000)
+    assert abs(int(nit[0]) - it_or) <= max(2, int(0.02 * it_or))

@@ -116,6 +116,11 @@ _SIGNATURES = {
     "gbpc_msolver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_msolver_device_bytes": [_vp, _szp],
     "gbpc_msolver_destroy": [_vp],
+    "gbpc_csolver_create": [_int, _vp, _vp, _vp, ctypes.POINTER(_vp)],
+    "gbpc_csolver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
+    "gbpc_csolver_cluster_size": [_vp, ctypes.POINTER(_int)],
+    "gbpc_csolver_device_bytes": [_vp, _szp],
+    "gbpc_csolver_destroy": [_vp],
 }
 
 _lock = threading.Lock()

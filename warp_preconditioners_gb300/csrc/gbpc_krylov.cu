@@ -181,12 +181,15 @@ namespace coop {
 namespace cgr = cooperative_groups;
 
 constexpr int kThreadsC = 256;  // 8 warps per CTA
-constexpr int kMaxRows = 65536;
-// Up to this many rows the solve runs on one thread-block cluster (16 CTAs,
-// or 8 where 16 cannot be scheduled): hardware cluster barriers and sums
-// exchanged through distributed shared memory.  Larger systems use a
-// cooperative grid of up to one CTA slot per resident CTA.
-constexpr int kClusterRows = 32768;
+// A system whose CG iteration needs at most this many multiply-adds (stored
+// entries of every product, padding included, plus the vector updates)
+// runs on one thread-block cluster of 16 CTAs (8 where 16 cannot be
+// scheduled): the cluster's FP64 rate covers it in a few microseconds, less
+// than the launches of the graph loop it replaces.  Measured: the 64 x 64
+// Laplacian with FSAI w8 (~114k) runs 13.7 against 27.7 us per iteration;
+// biharmonic systems of 15k-50k rows (0.7-2.2 M) ran slower on a cluster
+// than on the whole GPU.
+constexpr int64_t kClusterWork = 600000;
 
 struct Mat {
   int nrow, nslices;
@@ -206,7 +209,6 @@ struct Args {
   const double* b;
   double* x;
   double *r, *z, *p, *Ap, *t, *u;
-  double* partials;  // [2][gridDim.x]
   KrylovScalars* ks;
 };
 
@@ -216,12 +218,12 @@ enum CoopEpi : int { CE_PLAIN = 0, CE_SCALE = 1, CE_MASS = 2 };
 
 // z = m x (one warp per slice, rows in storage order); dot_part += z . w.
 __device__ __forceinline__ void product(const Mat& m, const double* x, double* z, const double* w,
-                                        double& dot_part, int epi = CE_PLAIN,
-                                        const double* aux0 = nullptr,
+                                        double& dot_part, int cta, int ncta,
+                                        int epi = CE_PLAIN, const double* aux0 = nullptr,
                                         const double* aux1 = nullptr) {
   const int lane = threadIdx.x & 31;
-  const int nwarps = gridDim.x * (kThreadsC / 32);
-  for (int s = blockIdx.x * (kThreadsC / 32) + (threadIdx.x >> 5); s < m.nslices; s += nwarps) {
+  const int nwarps = ncta * (kThreadsC / 32);
+  for (int s = cta * (kThreadsC / 32) + (threadIdx.x >> 5); s < m.nslices; s += nwarps) {
     const int64_t base = m.slice_ptr[s];
     const int width = (int)((m.slice_ptr[s + 1] - base) / kSlice);
     double acc = 0.0;
@@ -269,39 +271,11 @@ __device__ __forceinline__ double cta_sum(double v, double* sh) {
   return c;
 }
 
-// Synchronisation and the exchange of per-CTA sums, two ways.  Both return
-// the same total on every CTA: the CTA sums added in CTA order (lanes take
-// them strided, then a fixed butterfly).  Two slots alternate, so a CTA
-// that runs ahead never overwrites sums another CTA is still reading.
+// Synchronisation and the exchange of per-CTA sums.  Every CTA gets the
+// same total: the CTA sums added in CTA order (lanes take them strided,
+// then a fixed butterfly).  Two slots alternate, so a CTA that runs ahead
+// never overwrites sums another CTA is still reading.
 //
-// GridSync: any grid of co-resident CTAs (cooperative launch); the sums
-// go through global memory and grid syncs.
-struct GridSync {
-  cgr::grid_group g;
-  double* partials;  // [2][gridDim.x]
-  __device__ explicit GridSync(double* p) : g(cgr::this_grid()), partials(p) {}
-  __device__ void sync() { g.sync(); }
-  __device__ double total(double v, int slot, double* sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const double c = cta_sum(v, sh);
-    if (threadIdx.x == 0) partials[(size_t)slot * gridDim.x + blockIdx.x] = c;
-    g.sync();
-    if (warp == 0) {
-      double a = 0.0;
-      for (unsigned int q = lane; q < gridDim.x; q += 32)
-        a += __ldcg(partials + (size_t)slot * gridDim.x + q);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (lane == 0) sh[kThreadsC / 32] = a;
-    }
-    __syncthreads();
-    const double t = sh[kThreadsC / 32];
-    __syncthreads();
-    return t;
-  }
-  __device__ void finish() {}
-};
-
 // ClusterSync: the grid is one thread-block cluster; syncs are the
 // cluster's hardware barrier and every CTA reads the others' sums from
 // their shared memory (distributed shared memory), no global round trip.
@@ -336,14 +310,14 @@ struct ClusterSync {
 // Laplacian's two with a sync between them.
 template <class S>
 __device__ __forceinline__ void apply_a(S& grid, const Args& a, const double* x, double* out,
-                                        const double* w, double& dot_part) {
+                                        const double* w, double& dot_part, int cta, int ncta) {
   if (a.inv_mass) {
     double d0 = 0.0;
-    product(a.A, x, a.u, nullptr, d0, CE_SCALE, a.inv_mass);
+    product(a.A, x, a.u, nullptr, d0, cta, ncta, CE_SCALE, a.inv_mass);
     grid.sync();
-    product(a.A, a.u, out, w, dot_part, CE_MASS, a.wmass, x);
+    product(a.A, a.u, out, w, dot_part, cta, ncta, CE_MASS, a.wmass, x);
   } else {
-    product(a.A, x, out, w, dot_part);
+    product(a.A, x, out, w, dot_part, cta, ncta);
   }
 }
 
@@ -351,13 +325,13 @@ __device__ __forceinline__ void apply_a(S& grid, const Args& a, const double* x,
 // thread's share of r.z.
 template <class S>
 __device__ __forceinline__ double precondition(S& grid, const Args& a, bool precond, int64_t gt,
-                                               int64_t gs) {
+                                               int64_t gs, int cta, int ncta) {
   double prz = 0.0;
   if (precond) {
     double d0 = 0.0;
-    product(a.G, a.r, a.t, nullptr, d0);
+    product(a.G, a.r, a.t, nullptr, d0, cta, ncta);
     grid.sync();
-    product(a.GT, a.t, a.z, a.r, prz);
+    product(a.GT, a.t, a.z, a.r, prz, cta, ncta);
   } else {
     for (int64_t i = gt; i < a.n; i += gs) {
       const double ri = a.r[i];
@@ -368,18 +342,13 @@ __device__ __forceinline__ double precondition(S& grid, const Args& a, bool prec
   return prz;
 }
 
+// One system's PCG solve on CTAs cta = 0..ncta-1 of a grid or a cluster.
 template <class S>
-__global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
-  __shared__ double sh[kThreadsC / 32 + 1];
-  __shared__ double xch[2];
-  S grid = [&]() {
-    if constexpr (std::is_same<S, ClusterSync>::value) return S(xch);
-    else return S(a.partials);
-  }();
+__device__ void pcg_body(const Args& a, S& grid, int cta, int ncta, double* sh) {
   KrylovScalars* ks = a.ks;
   const int64_t n = a.n;
-  const int64_t gt = (int64_t)blockIdx.x * kThreadsC + threadIdx.x;
-  const int64_t gs = (int64_t)gridDim.x * kThreadsC;
+  const int64_t gt = (int64_t)cta * kThreadsC + threadIdx.x;
+  const int64_t gs = (int64_t)ncta * kThreadsC;
   const bool precond = a.G.nslices >= 0;
   int slot = 0;
   const double tol = ks->tol, atol = ks->atol;
@@ -388,7 +357,7 @@ __global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
   const int hist_len = ks->hist_len;
   // r = b - A x; b.b and r.r.
   double dummy = 0.0;
-  apply_a(grid, a, a.x, a.Ap, nullptr, dummy);
+  apply_a(grid, a, a.x, a.Ap, nullptr, dummy, cta, ncta);
   grid.sync();
   double pbb = 0.0, prr = 0.0;
   for (int64_t i = gt; i < n; i += gs) {
@@ -406,7 +375,7 @@ __global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
   const double atol_sq = at * at;
   if (gt == 0 && hist && hist_len > 0) hist[0] = sqrt(rr);
   // z = M r, rz = r.z, p = z.
-  double prz = precondition(grid, a, precond, gt, gs);
+  double prz = precondition(grid, a, precond, gt, gs, cta, ncta);
   double rz = grid.total(prz, slot, sh);
   slot ^= 1;
   for (int64_t i = gt; i < n; i += gs) a.p[i] = a.z[i];
@@ -415,7 +384,7 @@ __global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
   double alpha = 0.0, beta = 0.0, pap = 0.0;
   while (rr > atol_sq && it < maxiter) {
     double ppap = 0.0;
-    apply_a(grid, a, a.p, a.Ap, a.p, ppap);
+    apply_a(grid, a, a.p, a.Ap, a.p, ppap, cta, ncta);
     pap = grid.total(ppap, slot, sh);
     slot ^= 1;
     alpha = rz / pap;
@@ -429,7 +398,7 @@ __global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
     rr = grid.total(prr2, slot, sh);
     slot ^= 1;
     if (gt == 0 && hist && it + 1 < hist_len) hist[it + 1] = sqrt(rr);
-    const double prz2 = precondition(grid, a, precond, gt, gs);
+    const double prz2 = precondition(grid, a, precond, gt, gs, cta, ncta);
     const double rz_new = grid.total(prz2, slot, sh);
     slot ^= 1;
     beta = rz_new / rz;
@@ -452,6 +421,57 @@ __global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
   }
 }
 
+// One system on one cluster (the grid is that cluster).
+__global__ void __launch_bounds__(kThreadsC) pcg_kernel(Args a) {
+  __shared__ double sh[kThreadsC / 32 + 1];
+  __shared__ double xch[2];
+  ClusterSync grid(xch);
+  pcg_body(a, grid, blockIdx.x, gridDim.x, sh);
+}
+
+// Many systems in one launch: cluster c (CTAs c*C .. c*C+C-1 of a 1-D grid
+// of nsys clusters of C CTAs) solves system c with its own operator,
+// preconditioner, vectors and scalars.  Clusters never wait on each other:
+// each leaves when its own system has converged.
+__global__ void __launch_bounds__(kThreadsC) multi_cluster_kernel(const Args* systems, int nsys) {
+  __shared__ double sh[kThreadsC / 32 + 1];
+  __shared__ double xch[2];
+  cgr::cluster_group cl = cgr::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int sys = blockIdx.x / C;
+  if (sys >= nsys) return;  // uniform over a cluster
+  const Args a = systems[sys];
+  ClusterSync sync(xch);
+  pcg_body(a, sync, (int)cl.block_rank(), C, sh);
+}
+
+// tol, atol, maxiter (<= 0: the system's size) of every system, no history.
+__global__ void multi_set_kernel(const Args* systems, int nsys, double tol, double atol,
+                                 int maxiter) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  KrylovScalars* ks = systems[s].ks;
+  ks->tol = tol;
+  ks->atol = atol;
+  const int64_t n = systems[s].n;
+  ks->maxiter = maxiter > 0 ? maxiter : (n < 0x7fffffff ? (int)n : 0x7fffffff);
+  ks->it = 0;
+  ks->active = 1;
+  ks->cond_handle = 0ull;
+  ks->hist = nullptr;
+  ks->hist_len = 0;
+}
+
+__global__ void multi_outputs_kernel(const Args* systems, int nsys, int32_t* nit, double* rr,
+                                     double* atol_sq) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const KrylovScalars* ks = systems[s].ks;
+  if (nit) nit[s] = ks->it;
+  if (rr) rr[s] = ks->rr;
+  if (atol_sq) atol_sq[s] = ks->atol_sq;
+}
+
 Mat mat_of(const Sell& m) {
   return Mat{m.nrow, m.nslices, m.slice_ptr.as<int64_t>(), m.cols.as<int32_t>(),
              m.vals.as<double>(), m.perm.p ? m.perm.as<int32_t>() : nullptr};
@@ -463,6 +483,44 @@ bool enabled() {
     return !(e && e[0] == '0');
   }();
   return on;
+}
+
+// Cluster size both cluster kernels run with: 16 CTAs when such a cluster
+// of either kernel can be scheduled, else 8, else 0 (no cluster path).
+// One size for both, so a system gives the same bits alone and in a group.
+int cluster_size() {
+  static int chosen = -1;
+  if (chosen >= 0) return chosen;
+  chosen = 0;
+  const void* kerns[2] = {(const void*)pcg_kernel, (const void*)multi_cluster_kernel};
+  for (const void* k : kerns)
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      cudaGetLastError();
+  for (int c : {16, 8}) {
+    bool ok = true;
+    for (const void* k : kerns) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(kThreadsC);
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = c;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        ok = false;
+      }
+    }
+    if (ok) {
+      chosen = c;
+      break;
+    }
+  }
+  return chosen;
 }
 
 }  // namespace coop
@@ -483,13 +541,12 @@ struct Solver {
   double* hist = nullptr;  // residual history of the next runs (gbpc_solver_set_history)
   int hist_len = 0;
   bool use_pdl = true;  // programmatic dependent launches inside the loop body
-  // Small scalar systems (coop::kMaxRows) with a sparse operator and an
-  // FSAI or no preconditioner run as one cooperative kernel (coop_grid CTAs).
+  // Small systems (coop::kClusterWork) with a sparse or factored operator
+  // and an FSAI or no preconditioner run as one kernel on one cluster.
   bool coop = false;
-  int coop_grid = 0;
-  int coop_cluster = 0;  // > 0: the grid is one cluster of this many CTAs
+  int coop_cluster = 0;  // CTAs of that cluster
   coop::Args cargs{};
-  DevBuf r, z, p, Ap, Az, y, ks, zeros, t, u, cpart;
+  DevBuf r, z, p, Ap, Az, y, ks, zeros, t, u;
   ReduceBuf rb;
   // Cached graph for the last (b, x) pair.
   cudaGraphExec_t exec = nullptr;
@@ -712,9 +769,7 @@ struct Solver {
   // warp, at most what can be resident at once.
   int setup_coop() {
     coop = false;
-    if (!coop::enabled() || method != GBPC_CG || !use_graph || low || n > coop::kMaxRows ||
-        n < 1)
-      return GBPC_OK;
+    if (!coop::enabled() || method != GBPC_CG || !use_graph || low || n < 1) return GBPC_OK;
     const Sell* pa[1] = {nullptr};
     const Sell* pm[2] = {nullptr, nullptr};
     const void* inv_mass = nullptr;
@@ -722,48 +777,14 @@ struct Solver {
     if (A->scalar_products(pa, 1) != 1 && !A->factored_parts(pa, &inv_mass, &wmass))
       return GBPC_OK;
     if (M && M->scalar_products(pm, 2) != 2) return GBPC_OK;
-    int dev = 0, sms = 0, per_sm = 0;
-    GBPC_CUDA_TRY(cudaGetDevice(&dev));
-    GBPC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    GBPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, coop::pcg_kernel<coop::GridSync>, coop::kThreadsC, 0));
-    int coop_ok = 0;
-    GBPC_CUDA_TRY(cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, dev));
-    if (!coop_ok || per_sm < 1) return GBPC_OK;
-    const int warps = coop::kThreadsC / 32;
-    int need = (pa[0]->nslices + warps - 1) / warps;
-    if (M) need = std::max(need, std::max((pm[0]->nslices + warps - 1) / warps,
-                                          (pm[1]->nslices + warps - 1) / warps));
-    coop_grid = std::max(1, std::min(need, sms * per_sm));
-    coop_cluster = 0;
-    if (n <= coop::kClusterRows) {
-      auto kern = coop::pcg_kernel<coop::ClusterSync>;
-      if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-          cudaSuccess)
-        cudaGetLastError();
-      for (int c : {16, 8}) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(c);
-        cfg.blockDim = dim3(coop::kThreadsC);
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = c;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int clusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) == cudaSuccess && clusters > 0) {
-          coop_cluster = c;
-          break;
-        }
-        cudaGetLastError();
-      }
-    }
+    const int64_t work = (inv_mass ? 2 : 1) * pa[0]->nent +
+                         (M ? pm[0]->nent + pm[1]->nent : 0) + 8 * n;
+    if (work > coop::kClusterWork) return GBPC_OK;
+    coop_cluster = coop::cluster_size();
+    if (coop_cluster == 0) return GBPC_OK;
     int rc;
     if ((rc = t.alloc(sizeof(double) * n))) return rc;
     if (inv_mass && (rc = u.alloc(sizeof(double) * n))) return rc;
-    if ((rc = cpart.alloc(sizeof(double) * 2 * coop_grid))) return rc;
     cargs = coop::Args{};
     cargs.A = coop::mat_of(*pa[0]);
     cargs.inv_mass = (const double*)inv_mass;
@@ -782,7 +803,6 @@ struct Solver {
     cargs.p = p.as<double>();
     cargs.Ap = Ap.as<double>();
     cargs.t = t.as<double>();
-    cargs.partials = cpart.as<double>();
     cargs.ks = K();
     coop = true;
     return GBPC_OK;
@@ -798,24 +818,18 @@ struct Solver {
       coop::Args a = cargs;
       a.b = b;
       a.x = x;
-      if (coop_cluster > 0) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(coop_cluster);
-        cfg.blockDim = dim3(coop::kThreadsC);
-        cfg.stream = st;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = coop_cluster;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        GBPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, coop::pcg_kernel<coop::ClusterSync>, a));
-      } else {
-        void* params[] = {&a};
-        GBPC_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)coop::pcg_kernel<coop::GridSync>,
-                                                  coop_grid, coop::kThreadsC, params, 0, st));
-      }
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(coop_cluster);
+      cfg.blockDim = dim3(coop::kThreadsC);
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = coop_cluster;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      GBPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, coop::pcg_kernel, a));
     } else if (use_graph) {
       if (!exec || last_b != b || last_x != x) {
         rc = build_graph(b, x, st);
@@ -998,4 +1012,185 @@ extern "C" int gbpc_krylov(int method, gbpc_op* A, gbpc_op* M, const double* b, 
   }
   gbpc_solver_destroy(s);
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Many independent small systems in one launch, one thread-block cluster per
+// system (coop::multi_cluster_kernel).  Unlike gbpc_msolver, the systems keep
+// their own operators (nothing is concatenated), each cluster leaves as soon
+// as its system has converged, and a system's iterates are those of the
+// single-system cluster kernel of the same cluster size.
+
+
+struct gbpc_csolver {
+  size_t device_bytes = 0;  // declared first: released last
+  int nsys = 0;
+  int cluster = 0;
+  std::vector<coop::Args> host_args;
+  gbpc::DevBuf args, vecs, scalars;
+};
+
+extern "C" int gbpc_csolver_create(int nsys, gbpc_op* const* A, gbpc_op* const* M, void* stream,
+                                   gbpc_csolver** out) {
+  if (!out || nsys < 1 || !A) {
+    gbpc_set_error("gbpc_csolver_create: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  const int C = coop::cluster_size();
+  if (C == 0) {
+    gbpc_set_error("gbpc_csolver_create: no thread-block cluster of 8 or 16 CTAs can be scheduled");
+    return GBPC_ERR_UNSUPPORTED;
+  }
+  struct Parts {
+    const Sell* a;
+    const void* im;
+    const void* wm;
+    const Sell* g;
+    const Sell* gt;
+    int64_t n;
+  };
+  std::vector<Parts> parts((size_t)nsys);
+  size_t doubles = 0;
+  for (int s = 0; s < nsys; ++s) {
+    if (!A[s] || !A[s]->impl) {
+      gbpc_set_error("gbpc_csolver_create: system %d has no operator", s);
+      return GBPC_ERR_ARG;
+    }
+    Operator* a = A[s]->impl.get();
+    Operator* m = (M && M[s] && M[s]->impl) ? M[s]->impl.get() : nullptr;
+    Parts p{};
+    const Sell* pa[1] = {nullptr};
+    const Sell* pm[2] = {nullptr, nullptr};
+    if (a->scalar_products(pa, 1) != 1 && !a->factored_parts(pa, &p.im, &p.wm)) {
+      gbpc_set_error("gbpc_csolver_create: system %d: the operator must be a float64 scalar sparse "
+                     "product or the factored squared Laplacian with every vertex free", s);
+      return GBPC_ERR_UNSUPPORTED;
+    }
+    if (m && m->scalar_products(pm, 2) != 2) {
+      gbpc_set_error("gbpc_csolver_create: system %d: the preconditioner must be a float64 "
+                     "scalar FSAI or none", s);
+      return GBPC_ERR_UNSUPPORTED;
+    }
+    if (m && m->rows != a->rows) {
+      gbpc_set_error("gbpc_csolver_create: system %d: operator and preconditioner sizes differ", s);
+      return GBPC_ERR_ARG;
+    }
+    p.a = pa[0];
+    p.g = pm[0];
+    p.gt = pm[1];
+    p.n = a->rows;
+    doubles += (size_t)p.n * (p.im ? 6 : 5);
+    parts[s] = p;
+  }
+  auto* h = new gbpc_csolver;
+  ByteTally tally(&h->device_bytes);
+  h->nsys = nsys;
+  h->cluster = C;
+  int rc = h->vecs.alloc(sizeof(double) * std::max<size_t>(doubles, 1));
+  if (!rc) rc = h->scalars.alloc(sizeof(KrylovScalars) * nsys);
+  if (!rc) rc = h->args.alloc(sizeof(coop::Args) * nsys);
+  if (!rc && cudaMemsetAsync(h->scalars.p, 0, sizeof(KrylovScalars) * nsys, (cudaStream_t)stream) !=
+                 cudaSuccess)
+    rc = GBPC_ERR_CUDA;
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  h->host_args.resize((size_t)nsys);
+  double* v = h->vecs.as<double>();
+  for (int s = 0; s < nsys; ++s) {
+    const Parts& p = parts[s];
+    coop::Args& g = h->host_args[s];
+    g = coop::Args{};
+    g.A = coop::mat_of(*p.a);
+    if (p.g) {
+      g.G = coop::mat_of(*p.g);
+      g.GT = coop::mat_of(*p.gt);
+    } else {
+      g.G.nslices = -1;
+      g.GT.nslices = -1;
+    }
+    g.inv_mass = (const double*)p.im;
+    g.wmass = (const double*)p.wm;
+    g.n = p.n;
+    g.r = v;
+    g.z = v + p.n;
+    g.p = v + 2 * p.n;
+    g.Ap = v + 3 * p.n;
+    g.t = v + 4 * p.n;
+    g.u = p.im ? v + 5 * p.n : nullptr;
+    v += (size_t)p.n * (p.im ? 6 : 5);
+    g.ks = h->scalars.as<KrylovScalars>() + s;
+  }
+  *out = h;
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_csolver_run(gbpc_csolver* h, const double* const* b_host, double* const* x_host,
+                                double tol, double atol, int maxiter, int32_t* nit_dev,
+                                double* rr_dev, double* atol_sq_dev, void* stream) {
+  NvtxRange nvtx_range("gbpc_csolver_run");
+  if (!h || !b_host || !x_host) {
+    gbpc_set_error("gbpc_csolver_run: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int s = 0; s < h->nsys; ++s) {
+    if (h->host_args[s].n > 0 && (!b_host[s] || !x_host[s])) {
+      gbpc_set_error("gbpc_csolver_run: system %d has no right-hand side or solution vector", s);
+      return GBPC_ERR_ARG;
+    }
+    h->host_args[s].b = b_host[s];
+    h->host_args[s].x = x_host[s];
+  }
+  // Pageable source: the copy is staged before the call returns.
+  GBPC_CUDA_TRY(cudaMemcpyAsync(h->args.p, h->host_args.data(), sizeof(coop::Args) * h->nsys,
+                                cudaMemcpyHostToDevice, st));
+  const coop::Args* dargs = h->args.as<coop::Args>();
+  coop::multi_set_kernel<<<grid_for(h->nsys, 128), 128, 0, st>>>(dargs, h->nsys, tol, atol,
+                                                                 maxiter);
+  GBPC_CUDA_TRY(cudaGetLastError());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)h->nsys * h->cluster);
+  cfg.blockDim = dim3(coop::kThreadsC);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = h->cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  GBPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, coop::multi_cluster_kernel, dargs, h->nsys));
+  if (nit_dev || rr_dev || atol_sq_dev) {
+    coop::multi_outputs_kernel<<<grid_for(h->nsys, 128), 128, 0, st>>>(dargs, h->nsys, nit_dev,
+                                                                       rr_dev, atol_sq_dev);
+    GBPC_CUDA_TRY(cudaGetLastError());
+  }
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_csolver_cluster_size(const gbpc_csolver* h, int* cluster_host) {
+  if (!h || !cluster_host) {
+    gbpc_set_error("gbpc_csolver_cluster_size: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *cluster_host = h->cluster;
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_csolver_device_bytes(const gbpc_csolver* h, size_t* bytes_host) {
+  if (!h || !bytes_host) {
+    gbpc_set_error("gbpc_csolver_device_bytes: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *bytes_host = h->device_bytes;
+  return GBPC_OK;
+}
+
+extern "C" int gbpc_csolver_destroy(gbpc_csolver* h) {
+  if (!h) return GBPC_OK;
+  cudaDeviceSynchronize();
+  delete h;
+  return GBPC_OK;
 }
