@@ -369,6 +369,13 @@ int gbpc_solver_run(gbpc_solver* solver, const double* b, double* x, double tol,
  * iterates do not change.  Replaces the reference's diagnostic patch of
  * Warp's loop driver (benchmarks/residual_history.py:22-46). */
 int gbpc_solver_set_history(gbpc_solver* solver, double* hist, int hist_len);
+
+/* CTAs of the thread-block cluster that runs this solver's whole CG solve
+ * as one kernel (small systems: at most ~600k multiply-adds per iteration,
+ * a float64 scalar sparse or factored operator, an FSAI or no
+ * preconditioner), or 0 when it runs the graph loop of separate kernels.
+ * No reference counterpart. */
+int gbpc_solver_cluster(const gbpc_solver* solver, int* cluster_host);
 int gbpc_solver_destroy(gbpc_solver* solver);
 /* Device bytes of the solver's Krylov state (work vectors, scalars). */
 int gbpc_solver_device_bytes(const gbpc_solver* solver, size_t* bytes_host);
@@ -465,17 +472,18 @@ int gbpc_msolver_destroy(gbpc_msolver* solver);
  * Laplacian with every vertex free) preconditioned by M[s] (a float64
  * scalar FSAI, or NULL).  Nothing is concatenated; each cluster stops when
  * its own system passes the stopping test (r.r <= max(atol, tol |b_s|)^2,
- * or maxiter; maxiter <= 0 means the system's size).  b_host / x_host are
- * host arrays of nsys device pointers; nit_dev / rr_dev / atol_sq_dev hold
- * nsys entries (any may be NULL).  A system's iterates equal those of the
+ * or maxiter; maxiter <= 0 means the system's size).  A run solves systems
+ * 0 .. count-1 (count <= nsys); b_host / x_host are host arrays of count
+ * device pointers; nit_dev / rr_dev / atol_sq_dev hold count entries (any
+ * may be NULL).  A system's iterates equal those of the
  * single-system cluster kernel that gbpc_solver uses for CG below 32,768
  * rows.  Stream-ordered.  No reference counterpart. */
 typedef struct gbpc_csolver gbpc_csolver;
 int gbpc_csolver_create(int nsys, gbpc_op* const* A, gbpc_op* const* M, void* stream,
                         gbpc_csolver** out);
-int gbpc_csolver_run(gbpc_csolver* solver, const double* const* b_host, double* const* x_host,
-                     double tol, double atol, int maxiter, int32_t* nit_dev, double* rr_dev,
-                     double* atol_sq_dev, void* stream);
+int gbpc_csolver_run(gbpc_csolver* solver, int count, const double* const* b_host,
+                     double* const* x_host, double tol, double atol, int maxiter,
+                     int32_t* nit_dev, double* rr_dev, double* atol_sq_dev, void* stream);
 int gbpc_csolver_cluster_size(const gbpc_csolver* solver, int* cluster_host);
 int gbpc_csolver_device_bytes(const gbpc_csolver* solver, size_t* bytes_host);
 int gbpc_csolver_destroy(gbpc_csolver* solver);

@@ -89,6 +89,7 @@ _SIGNATURES = {
     "gbpc_solver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_solver_destroy": [_vp],
     "gbpc_solver_set_history": [_vp, _vp, _int],
+    "gbpc_solver_cluster": [_vp, ctypes.POINTER(_int)],
     "gbpc_solver_device_bytes": [_vp, _szp],
     "gbpc_gmres_create": [_vp, _vp, _int, _vp, ctypes.POINTER(_vp)],
     "gbpc_gmres_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _int, _vp, _vp, _vp, _vp],
@@ -117,7 +118,7 @@ _SIGNATURES = {
     "gbpc_msolver_device_bytes": [_vp, _szp],
     "gbpc_msolver_destroy": [_vp],
     "gbpc_csolver_create": [_int, _vp, _vp, _vp, ctypes.POINTER(_vp)],
-    "gbpc_csolver_run": [_vp, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
+    "gbpc_csolver_run": [_vp, _int, _vp, _vp, _dbl, _dbl, _int, _vp, _vp, _vp, _vp],
     "gbpc_csolver_cluster_size": [_vp, ctypes.POINTER(_int)],
     "gbpc_csolver_device_bytes": [_vp, _szp],
     "gbpc_csolver_destroy": [_vp],

@@ -952,6 +952,15 @@ extern "C" int gbpc_solver_run(gbpc_solver* h, const double* b, double* x, doubl
   return h->s.run(b, x, tol, atol, maxiter, nit_dev, rr_dev, atol_sq_dev, (cudaStream_t)stream);
 }
 
+extern "C" int gbpc_solver_cluster(const gbpc_solver* h, int* cluster_host) {
+  if (!h || !cluster_host) {
+    gbpc_set_error("gbpc_solver_cluster: bad arguments");
+    return GBPC_ERR_ARG;
+  }
+  *cluster_host = h->s.coop ? h->s.coop_cluster : 0;
+  return GBPC_OK;
+}
+
 extern "C" int gbpc_solver_set_history(gbpc_solver* h, double* hist, int hist_len) {
   if (!h || hist_len < 0 || (hist_len > 0 && !hist)) {
     gbpc_set_error("gbpc_solver_set_history: bad arguments");
@@ -1126,16 +1135,17 @@ extern "C" int gbpc_csolver_create(int nsys, gbpc_op* const* A, gbpc_op* const* 
   return GBPC_OK;
 }
 
-extern "C" int gbpc_csolver_run(gbpc_csolver* h, const double* const* b_host, double* const* x_host,
-                                double tol, double atol, int maxiter, int32_t* nit_dev,
-                                double* rr_dev, double* atol_sq_dev, void* stream) {
+extern "C" int gbpc_csolver_run(gbpc_csolver* h, int count, const double* const* b_host,
+                                double* const* x_host, double tol, double atol, int maxiter,
+                                int32_t* nit_dev, double* rr_dev, double* atol_sq_dev,
+                                void* stream) {
   NvtxRange nvtx_range("gbpc_csolver_run");
-  if (!h || !b_host || !x_host) {
+  if (!h || !b_host || !x_host || count < 1 || count > h->nsys) {
     gbpc_set_error("gbpc_csolver_run: bad arguments");
     return GBPC_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  for (int s = 0; s < h->nsys; ++s) {
+  for (int s = 0; s < count; ++s) {
     if (h->host_args[s].n > 0 && (!b_host[s] || !x_host[s])) {
       gbpc_set_error("gbpc_csolver_run: system %d has no right-hand side or solution vector", s);
       return GBPC_ERR_ARG;
@@ -1144,14 +1154,13 @@ extern "C" int gbpc_csolver_run(gbpc_csolver* h, const double* const* b_host, do
     h->host_args[s].x = x_host[s];
   }
   // Pageable source: the copy is staged before the call returns.
-  GBPC_CUDA_TRY(cudaMemcpyAsync(h->args.p, h->host_args.data(), sizeof(coop::Args) * h->nsys,
+  GBPC_CUDA_TRY(cudaMemcpyAsync(h->args.p, h->host_args.data(), sizeof(coop::Args) * count,
                                 cudaMemcpyHostToDevice, st));
   const coop::Args* dargs = h->args.as<coop::Args>();
-  coop::multi_set_kernel<<<grid_for(h->nsys, 128), 128, 0, st>>>(dargs, h->nsys, tol, atol,
-                                                                 maxiter);
+  coop::multi_set_kernel<<<grid_for(count, 128), 128, 0, st>>>(dargs, count, tol, atol, maxiter);
   GBPC_CUDA_TRY(cudaGetLastError());
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)h->nsys * h->cluster);
+  cfg.gridDim = dim3((unsigned)count * h->cluster);
   cfg.blockDim = dim3(coop::kThreadsC);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -1161,10 +1170,10 @@ extern "C" int gbpc_csolver_run(gbpc_csolver* h, const double* const* b_host, do
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  GBPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, coop::multi_cluster_kernel, dargs, h->nsys));
+  GBPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, coop::multi_cluster_kernel, dargs, count));
   if (nit_dev || rr_dev || atol_sq_dev) {
-    coop::multi_outputs_kernel<<<grid_for(h->nsys, 128), 128, 0, st>>>(dargs, h->nsys, nit_dev,
-                                                                       rr_dev, atol_sq_dev);
+    coop::multi_outputs_kernel<<<grid_for(count, 128), 128, 0, st>>>(dargs, count, nit_dev,
+                                                                     rr_dev, atol_sq_dev);
     GBPC_CUDA_TRY(cudaGetLastError());
   }
   return GBPC_OK;

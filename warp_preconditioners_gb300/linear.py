@@ -128,6 +128,15 @@ class Solver:
         """Device bytes of the Krylov state (work vectors and scalars)."""
         return _lib.object_bytes("gbpc_solver_device_bytes", self._h)
 
+    @property
+    def cluster_size(self) -> int:
+        """CTAs of the thread-block cluster that runs the whole solve as one
+        kernel (small systems), 0 when the graph loop of separate kernels
+        runs it."""
+        c = ctypes.c_int()
+        _lib.call("gbpc_solver_cluster", self._h, ctypes.byref(c))
+        return int(c.value)
+
     def run(self, b, x, tol=None, atol=None, maxiter=0, history=None):
         """Solve from the initial guess in x.  ``history`` (float64 device
         tensor, optional) receives |r_k| for k < len(history), k = 0 the

@@ -137,12 +137,14 @@ class ClusterSolver:
 
     def run(self, bs, xs, tol=None, atol=None, maxiter=0):
         """Solve system s for bs[s] from the initial guess xs[s] (float64
-        device tensors); returns device arrays (iterations, r.r, atol^2),
-        one entry per system.  Stream-ordered, no synchronisation."""
-        S = len(self.systems)
-        if len(bs) != S or len(xs) != S:
-            raise ValueError(f"expected {S} right-hand sides and {S} solution vectors")
-        for (a, _), b, x in zip(self.systems, bs, xs):
+        device tensors) for the first len(bs) systems; returns device arrays
+        (iterations, r.r, atol^2), one entry per system solved.
+        Stream-ordered, no synchronisation."""
+        S = len(bs)
+        if not 1 <= S <= len(self.systems) or len(xs) != S:
+            raise ValueError(f"expected 1..{len(self.systems)} right-hand sides and as many "
+                             f"solution vectors")
+        for (a, _), b, x in zip(self.systems[:S], bs, xs):
             if b.dtype != torch.float64 or x.dtype != torch.float64:
                 raise TypeError("the cluster solver runs on float64 vectors")
             if b.numel() != a.shape[0] or x.numel() != a.shape[0]:
@@ -151,7 +153,7 @@ class ClusterSolver:
         atol = 0.0 if atol is None else float(atol)
         bp = (ctypes.c_void_p * S)(*[_lib.ptr(_flat(b)).value for b in bs])
         xp = (ctypes.c_void_p * S)(*[_lib.ptr(_flat(x)).value for x in xs])
-        _lib.call("gbpc_csolver_run", self._h, bp, xp, tol, atol, int(maxiter),
+        _lib.call("gbpc_csolver_run", self._h, S, bp, xp, tol, atol, int(maxiter),
                   _lib.ptr(self.nit), _lib.ptr(self.rr), _lib.ptr(self.atol_sq),
                   _lib.stream(self.device))
-        return self.nit, self.rr, self.atol_sq
+        return self.nit[:S], self.rr[:S], self.atol_sq[:S]

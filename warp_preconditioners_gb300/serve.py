@@ -9,7 +9,9 @@ that cannot fit at all is rejected) and runs requests in slots, one CUDA
 stream each.  A free slot takes the oldest queued request whose system is
 idle, copies its right-hand sides in, runs the whole PCG loop as one CUDA
 graph (k > 1: the batched solver, which reads the matrices once per
-iteration for all k right-hand sides; k = 1: the single-vector solver),
+iteration for all k right-hand sides; k = 1: the single-vector solver; a
+small system's solves run on thread-block clusters instead, one kernel for
+the whole solve, one cluster per right-hand side in one launch),
 copies x back, and is free for the next request as soon as its event fires.
 Requests join and leave the running set one by one, so none waits for a
 batch to fill or for an unrelated long solve.
@@ -246,7 +248,17 @@ class ResidentSystem:
         self.B = torch.zeros(n * max_rhs, dtype=torch.float64, device=dev)
         self.X = torch.zeros(n * max_rhs, dtype=torch.float64, device=dev)
         self.bcg = None
-        if batched and max_rhs > 1:
+        self.csolver = None
+        if batched and max_rhs > 1 and self.solver.cluster_size > 0:
+            # A small system: its single-vector solve runs on one thread-block
+            # cluster, so the k right-hand sides of a request run as k such
+            # solves in one launch, each the single-vector result bit for bit.
+            from .multi import ClusterSolver
+
+            self.csolver = ClusterSolver([(self.A, self.fsai)] * max_rhs)
+            self.BT = torch.zeros((max_rhs, n), dtype=torch.float64, device=dev)
+            self.XT = torch.zeros((max_rhs, n), dtype=torch.float64, device=dev)
+        elif batched and max_rhs > 1:
             if host.kind == "laplacian":
                 BA = batched_sparse(A)
             else:
@@ -283,6 +295,13 @@ class ResidentSystem:
                 nit, _, _ = self.solver.run(self.b1, self.x1, tol, 0.0, maxiter)
                 out.view(-1).copy_(self.x1, non_blocking=True)
                 nit_out.copy_(nit, non_blocking=True)
+            elif self.csolver is not None and not sequential:
+                self.BT[:k].copy_(rhs.to(self.BT.device, non_blocking=True).t())
+                self.XT[:k].zero_()
+                nit, _, _ = self.csolver.run(list(self.BT[:k]), list(self.XT[:k]), tol, 0.0,
+                                             maxiter)
+                out.copy_(self.XT[:k].t(), non_blocking=True)
+                nit_out.copy_(nit, non_blocking=True)
             elif sequential or self.bcg is None:
                 B, X = self._blocks(k)
                 B.copy_(rhs, non_blocking=True)
@@ -313,11 +332,28 @@ class ResidentSystem:
         counts go back to each request's buffers."""
         ks = [int(r.shape[1]) for r in rhss]
         k = sum(ks)
-        if len(rhss) == 1 or k == 1 or self.bcg is None:
+        if len(rhss) == 1 or k == 1 or (self.bcg is None and self.csolver is None):
             raise ValueError("launch_group takes two or more requests on a batched system")
         if k > self.max_rhs or any(int(r.shape[0]) != self.n for r in rhss):
             raise ValueError(f"request group of {k} right-hand sides does not fit system "
                              f"{self.key} (n={self.n}, k <= {self.max_rhs})")
+        if self.csolver is not None:
+            with torch.cuda.stream(stream):
+                c = 0
+                for rhs, kk in zip(rhss, ks):
+                    self.BT[c:c + kk].copy_(rhs.to(self.BT.device, non_blocking=True).t())
+                    c += kk
+                self.XT[:k].zero_()
+                nit, _, _ = self.csolver.run(list(self.BT[:k]), list(self.XT[:k]), tol, 0.0,
+                                             maxiter)
+                c = 0
+                for out, kk in zip(outs, ks):
+                    out.copy_(self.XT[c:c + kk].t(), non_blocking=True)
+                    c += kk
+                nit_out.copy_(nit, non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(stream)
+            return ev
         with torch.cuda.stream(stream):
             B, X = self._blocks(k)
             c = 0
