@@ -78,6 +78,9 @@ def parse_args():
     p.add_argument("--c5-merge", type=int, default=0,
                    help="also serve with queued requests of one system merged into batched "
                         "solves of up to this many right-hand sides (0: skip that arm)")
+    p.add_argument("--c5-batched-small", action="store_true",
+                   help="also serve with small systems' multi-RHS requests on the batched "
+                        "solver instead of one cluster per right-hand side")
     p.add_argument("--c5-budget-gb", type=float, default=120.0)
     p.add_argument("--c5-nmin", type=float, default=5e3)
     p.add_argument("--c5-nmax", type=float, default=5e5)
@@ -1332,6 +1335,15 @@ def run_c5(args, dev):
         out["served_merged"] = serve.summarize(msrv.run(stream, keep=lambda r: False))
         out["served_merged_burst"] = serve.summarize(msrv.run(burst, keep=lambda r: False))
         del msrv, mex
+    if args.c5_batched_small:
+        bex = serve.GpuExecutor(cat, slots=args.c5_slots, tol=args.rtol, device=dev,
+                                cluster_rhs=False)
+        bsrv = serve.Server(bex, budget_bytes=budget)
+        bsrv.prepare(keys)
+        torch.cuda.synchronize()
+        out["served_batched_small"] = serve.summarize(bsrv.run(stream, keep=lambda r: False))
+        out["served_batched_small_burst"] = serve.summarize(bsrv.run(burst, keep=lambda r: False))
+        del bsrv, bex
     if not args.c5_no_sequential:
         seq_ex = serve.GpuExecutor(cat, sequential=True, tol=args.rtol, device=dev)
         seq = serve.Server(seq_ex, budget_bytes=budget)
@@ -1342,6 +1354,11 @@ def run_c5(args, dev):
         sb, qb = out["served_burst"], out["sequential_burst"]
         out["speedup"] = {"capacity_solves_per_s": sb["solves_per_s"] / qb["solves_per_s"],
                           "p50": q["p50_ms"] / s["p50_ms"], "p99": q["p99_ms"] / s["p99_ms"]}
+        if args.c5_batched_small:
+            mb, m = out["served_batched_small_burst"], out["served_batched_small"]
+            out["speedup_batched_small"] = {
+                "capacity_solves_per_s": mb["solves_per_s"] / qb["solves_per_s"],
+                "p50": q["p50_ms"] / m["p50_ms"], "p99": q["p99_ms"] / m["p99_ms"]}
         if args.c5_merge:
             mb, m = out["served_merged_burst"], out["served_merged"]
             out["speedup_merged"] = {

@@ -664,6 +664,387 @@ fsai_build_lanes_kernel(BuildParams P, const int32_t* __restrict__ off,
 }
 
 // ---------------------------------------------------------------------------
+// Wide rows (W > 16) by rounds.  A round is one growth step of every row
+// still growing, in two launches:
+//   * scoring, a warp per row: the row's support goes into a shared-memory
+//     hash table (marked with its position), the frontier's residuals are
+//     summed in support order as above, the step's candidates are selected,
+//     and each candidate's entries against the support (and against the
+//     candidates selected before it) are gathered from its own row;
+//   * factoring, a thread per row: the bordered Cholesky step for each
+//     candidate, then L^T z = v, and the stop tests.
+// The row's factor (packed by rows: L(r, p) at r(r+1)/2 + p), v and the
+// gathered entries live in device memory as structures of arrays over the
+// rows of a chunk, so the threads of a warp read consecutive words; w and z
+// live in shared memory, one column per thread.  The scoring tables alone
+// set how many warps fit on an SM, and the factor arithmetic, sequential
+// within a row, runs 32 rows to a warp.  The bordering's sums are the
+// reference's own left-looking loop (row p of L against w); every product
+// and sum is the reference's, in its order.  Rows still growing are kept in
+// a device list, rebuilt by the factor launch each round, so no round waits
+// on the host.
+
+template <typename T>
+struct RoundState {
+  int nc;           // rows in the chunk
+  int r0;           // first row of the chunk
+  int W, S;         // width; candidates per round (<= W)
+  int H, hbits;     // scoring table slots
+  int32_t* size;    // [nc] support size
+  int32_t* nsel;    // [nc] candidates selected this round
+  int32_t* flags;   // [nc] bit 0: truncated; bit 1: table overflow
+  int32_t* pat;     // [nc][W] support in insertion order
+  int32_t* cand;    // [nc][S]
+  T* z;             // [nc][W]
+  T* v;             // [W][nc]
+  T* L;             // [W(W+1)/2][nc]
+  T* a;             // [S][W][nc]: entries of candidate k against position p
+  int32_t* list0;   // rows still growing (chunk-local), two lists used in turn
+  int32_t* list1;
+  int32_t* count;   // [2] lengths of the lists
+};
+
+__host__ __device__ constexpr size_t round_smem_per_warp(int T_size, int H) {
+  return ((size_t)H * (T_size + sizeof(int) + 1) + 15) & ~(size_t)15;
+}
+
+template <typename T>
+__global__ void fsai_round_init_kernel(RoundState<T> R) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0) {
+    R.count[0] = R.nc;
+    R.count[1] = 0;
+  }
+  if (j >= R.nc) return;
+  const int i = R.r0 + j;
+  R.size[j] = 1;
+  R.nsel[j] = 0;
+  R.flags[j] = 0;
+  R.pat[(size_t)j * R.W] = i;
+  R.z[(size_t)j * R.W] = T(1);
+  R.v[j] = T(1);
+  R.L[j] = T(1);
+  R.list0[j] = j;
+}
+
+// Find or insert column c; `fresh` tells whether this call inserted it.
+__device__ __forceinline__ int hfind_insert_fresh(int* hkey, int hmask, int hbits, int c,
+                                                  bool& fresh) {
+  unsigned int s = hash_col(c) >> (32 - hbits);
+  fresh = false;
+  for (int probe = 0; probe <= hmask; ++probe) {
+    int k = hkey[s];
+    if (k == c) return (int)s;
+    if (k == kEmpty) {
+      k = atomicCAS(hkey + s, kEmpty, c);
+      if (k == kEmpty) {
+        fresh = true;
+        return (int)s;
+      }
+      if (k == c) return (int)s;
+    }
+    s = (s + 1) & hmask;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ int hfind(const int* hkey, int hmask, int hbits, int c) {
+  unsigned int s = hash_col(c) >> (32 - hbits);
+  for (int probe = 0; probe <= hmask; ++probe) {
+    const int k = hkey[s];
+    if (k == c) return (int)s;
+    if (k == kEmpty) return -1;
+    s = (s + 1) & hmask;
+  }
+  return -1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+fsai_round_score_kernel(RoundState<T> R, int cur, const int32_t* __restrict__ off,
+                        const int32_t* __restrict__ col, const T* __restrict__ ahat,
+                        const T* __restrict__ ahatT, int32_t* overflow_list,
+                        int32_t* overflow_count) {
+  extern __shared__ __align__(16) unsigned char round_smem[];
+  using BitsT = Bits<T>;
+  using U = typename BitsT::U;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int W = R.W, S = R.S, H = R.H, hbits = R.hbits, hmask = H - 1;
+  const int64_t nc = R.nc;
+  unsigned char* base = round_smem + (size_t)warp * round_smem_per_warp((int)sizeof(T), H);
+  T* hacc = reinterpret_cast<T*>(base);                    // [H] residuals
+  int* hkey = reinterpret_cast<int*>(hacc + H);            // [H] columns
+  signed char* hpos = reinterpret_cast<signed char*>(hkey + H);  // [H] see below
+  // hpos: 0 a candidate; p + 1 the support column at position p; -(k + 1)
+  // the k-th candidate selected this round.
+  if (blockIdx.x == 0 && threadIdx.x == 0) R.count[cur ^ 1] = 0;
+  const int count = R.count[cur];
+  const int32_t* list = cur ? R.list1 : R.list0;
+  for (int idx = blockIdx.x * nw + warp; idx < count; idx += gridDim.x * nw) {
+    const int j = list[idx];
+    const int i = R.r0 + j;
+    const int size = R.size[j];
+    // The support, its z and its rows' extents, two positions per lane.
+    int pc[2], ob[2], oe[2];
+    T zv[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int p = lane + 32 * h;
+      pc[h] = -1;
+      ob[h] = oe[h] = 0;
+      zv[h] = T(0);
+      if (p < size) {
+        pc[h] = R.pat[(size_t)j * W + p];
+        zv[h] = R.z[(size_t)j * W + p];
+        ob[h] = off[pc[h]];
+        oe[h] = off[pc[h] + 1];
+      }
+    }
+    for (int s = lane; s < H; s += 32) hkey[s] = kEmpty;
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (pc[h] >= 0) {
+        bool fresh;
+        const int s = hfind_insert_fresh(hkey, hmask, hbits, pc[h], fresh);
+        if (s >= 0) hpos[s] = (signed char)(lane + 32 * h + 1);  // H > W: always found
+      }
+    }
+    __syncwarp();
+    // Frontier residuals, summed in support order.
+    bool overflow = false;
+    for (int q = 0; q < size; ++q) {
+      const int h = q >> 5, src = q & 31;
+      const int b = __shfl_sync(0xffffffffu, h ? ob[1] : ob[0], src);
+      const int e_end = __shfl_sync(0xffffffffu, h ? oe[1] : oe[0], src);
+      const T zq = __shfl_sync(0xffffffffu, h ? zv[1] : zv[0], src);
+      for (int e = b + lane; e < e_end; e += 32) {
+        const int c = col[e];
+        if (c >= i) continue;
+        bool fresh;
+        const int s = hfind_insert_fresh(hkey, hmask, hbits, c, fresh);
+        if (s < 0) {
+          overflow = true;
+        } else if (fresh) {
+          hpos[s] = 0;
+          hacc[s] = ahatT[e] * zq;  // 0 + t: the same magnitude, which is all the score reads
+        } else if (hpos[s] == 0) {
+          const T t = ahatT[e] * zq;
+          hacc[s] = hacc[s] + t;
+        }
+      }
+      __syncwarp();
+    }
+    if (__any_sync(0xffffffffu, overflow)) {
+      if (lane == 0) {
+        R.flags[j] |= 2;
+        R.nsel[j] = 0;
+        overflow_list[atomicAdd(overflow_count, 1)] = i;
+      }
+      continue;
+    }
+    // Top candidates: higher score, then lower column.
+    const int want = min(S, W - size);
+    int ns = 0;
+    for (int k = 0; k < want; ++k) {
+      U best_bits = 0;
+      int best_col = 0x7fffffff;
+      int best_slot = -1;
+      for (int s = lane; s < H; s += 32) {
+        const int kk = hkey[s];
+        if (kk < 0 || hpos[s] != 0) continue;
+        const U bits = BitsT::abs_bits(hacc[s]);
+        if (bits == 0 || bits > BitsT::kInf) continue;  // zero or NaN: never selected
+        if (bits > best_bits || (bits == best_bits && kk < best_col)) {
+          best_bits = bits;
+          best_col = kk;
+          best_slot = s;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const U ob2 = __shfl_xor_sync(0xffffffffu, best_bits, o);
+        const int oc = __shfl_xor_sync(0xffffffffu, best_col, o);
+        const int os = __shfl_xor_sync(0xffffffffu, best_slot, o);
+        if (ob2 > best_bits || (ob2 == best_bits && oc < best_col)) {
+          best_bits = ob2;
+          best_col = oc;
+          best_slot = os;
+        }
+      }
+      if (best_slot < 0) break;
+      if (lane == 0) {
+        hpos[best_slot] = (signed char)(-(k + 1));
+        R.cand[(size_t)j * S + k] = best_col;
+      }
+      __syncwarp();
+      ++ns;
+    }
+    // Entries of each candidate against the support and the candidates
+    // selected before it; zero where the matrix stores none.
+    for (int k = 0; k < ns; ++k)
+      for (int p = lane; p < size + k; p += 32) R.a[((size_t)k * W + p) * nc + j] = T(0);
+    __syncwarp();
+    for (int k = 0; k < ns; ++k) {
+      const int best = R.cand[(size_t)j * S + k];
+      const int e_end = off[best + 1];
+      for (int e = off[best] + lane; e < e_end; e += 32) {
+        const int s = hfind(hkey, hmask, hbits, col[e]);
+        if (s < 0) continue;
+        const int hp = hpos[s];
+        int pos = -1;
+        if (hp > 0) pos = hp - 1;
+        else if (hp < 0 && -hp - 1 < k) pos = size + (-hp - 1);
+        if (pos >= 0) R.a[((size_t)k * W + pos) * nc + j] = ahat[e];
+      }
+    }
+    if (lane == 0) R.nsel[j] = ns;
+    __syncwarp();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+fsai_round_factor_kernel(RoundState<T> R, int cur, T tolerance, T pivot_floor) {
+  extern __shared__ __align__(16) unsigned char round_fsmem[];
+  T* ws = reinterpret_cast<T*>(round_fsmem);  // [W][blockDim.x]: w, then z
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  const int W = R.W, S = R.S;
+  const int64_t nc = R.nc;
+  const int count = R.count[cur];
+  const int32_t* list = cur ? R.list1 : R.list0;
+  int32_t* next = cur ? R.list0 : R.list1;
+  T* w = ws + tid;
+  for (int wbase = blockIdx.x * nt + (tid & ~31); wbase < count; wbase += gridDim.x * nt) {
+    const int idx = wbase + lane;
+    bool keep = false;
+    int j = -1;
+    if (idx < count) {
+      j = list[idx];
+      const int ns = R.nsel[j];
+      if (ns > 0) {
+        int size = R.size[j];
+        T* Lj = R.L + j;
+        const T* vj = R.v + j;
+        auto L = [&](int r, int p) -> T& { return Lj[((size_t)(r * (r + 1) / 2 + p)) * nc]; };
+        const T old_z0 = R.z[(size_t)j * W];
+        bool stopped = false;
+        for (int k = 0; k < ns; ++k) {
+          if (size == W) break;
+          const T* ak = R.a + (size_t)k * W * nc + j;
+          T pivot = T(1);
+          T rhs = T(0);
+          for (int p = 0; p < size; ++p) {
+            T acc = ak[(size_t)p * nc];
+            for (int q = 0; q < p; ++q) {
+              const T t = L(p, q) * w[q * nt];
+              acc = acc - t;
+            }
+            const T wp = acc / L(p, p);
+            w[p * nt] = wp;
+            const T sq = wp * wp;
+            pivot = pivot - sq;
+            const T pr = wp * vj[(size_t)p * nc];
+            rhs = rhs - pr;
+          }
+          if (pivot <= pivot_floor || !isfinite(pivot)) {
+            stopped = true;
+            break;
+          }
+          for (int p = 0; p < size; ++p) L(size, p) = w[p * nt];
+          R.pat[(size_t)j * W + size] = R.cand[(size_t)j * S + k];
+          const T d = sqrt(pivot);
+          L(size, size) = d;
+          R.v[(size_t)size * nc + j] = rhs / d;
+          ++size;
+        }
+        // L^T z = v, in the reference's order.
+        for (int p = size - 1; p >= 0; --p) {
+          T acc = vj[(size_t)p * nc];
+          for (int q = p + 1; q < size; ++q) {
+            const T t = L(q, p) * w[q * nt];
+            acc = acc - t;
+          }
+          w[p * nt] = acc / L(p, p);
+        }
+        for (int p = 0; p < size; ++p) R.z[(size_t)j * W + p] = w[p * nt];
+        R.size[j] = size;
+        if (stopped) {
+          R.flags[j] |= 1;
+        } else if (tolerance > T(0) && T(1) - old_z0 / w[0] <= tolerance) {
+          // converged
+        } else {
+          keep = size < W;
+        }
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int at = 0;
+    if (lane == 0 && m) at = atomicAdd(R.count + (cur ^ 1), __popc(m));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (keep) next[at + __popc(m & ((1u << lane) - 1u))] = j;
+  }
+}
+
+// Normalise, validate, sort by column and write the ELL rows of a chunk;
+// a warp per row.
+template <typename T>
+__global__ void __launch_bounds__(256)
+fsai_round_finish_kernel(RoundState<T> R, const T* __restrict__ scale, int32_t* ell_cols,
+                         T* ell_vals, int32_t* row_counts, int32_t* status) {
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= R.nc) return;
+  const int flags = R.flags[j];
+  if (flags & 2) return;  // rerun by the warp-per-row kernel
+  const int W = R.W, i = R.r0 + j, size = R.size[j];
+  const T norm = sqrt(R.z[(size_t)j * W]);
+  int my_col[2];
+  T my_val[2];
+  bool valid = true;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int p = lane + 32 * h;
+    my_col[h] = -1;
+    my_val[h] = T(0);
+    if (p < size) {
+      const int c = R.pat[(size_t)j * W + p];
+      const T t = R.z[(size_t)j * W + p] / norm;
+      const T val = t * scale[c];
+      my_col[h] = c;
+      my_val[h] = val;
+      if (!isfinite(val)) valid = false;
+      if (p == 0 && !(val > T(0))) valid = false;
+    }
+  }
+  const bool all_valid = __all_sync(0xffffffffu, valid);
+  int rank[2] = {0, 0};
+  for (int q = 0; q < size; ++q) {
+    const int cq = __shfl_sync(0xffffffffu, q < 32 ? my_col[0] : my_col[1], q & 31);
+    rank[0] += (cq < my_col[0]);
+    rank[1] += (cq < my_col[1]);
+  }
+  int32_t* oc = ell_cols + (size_t)i * W;
+  T* ov = ell_vals + (size_t)i * W;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int p = lane + 32 * h;
+    if (p < size) {
+      oc[rank[h]] = my_col[h];
+      ov[rank[h]] = my_val[h];
+    } else if (p < W) {
+      oc[p] = -1;
+      ov[p] = T(0);
+    }
+  }
+  if (lane == 0) {
+    row_counts[i] = size;
+    if (flags & 1) atomicAdd(status + 1, 1);
+    if (!all_valid) atomicAdd(status + 2, 1);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Scans, packing, transpose, scalarise, conversion.
 
 // Exclusive scan of int32 counts into out[0..n] (out[n] = total), 1024 per CTA.
@@ -1051,6 +1432,14 @@ static bool lanes_build_enabled() {
   return on;
 }
 
+static bool rounds_build_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBPC_FSAI_ROUNDS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <typename T>
 static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* val, int W,
                         int S, double kap, double floor_, int32_t* ell_cols, T* ell_vals,
@@ -1167,7 +1556,84 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
   };
-  if (W <= 48 && lanes_build_enabled()) {
+  // Widths above 16: the build by rounds (see fsai_round_score_kernel).
+  auto launch_rounds = [&](int H, int hbits) -> int {
+    const int SE = std::min(S, W);
+    const size_t per_warp = round_smem_per_warp((int)sizeof(T), H);
+    const int wpc = 4;
+    const size_t score_smem = per_warp * wpc;
+    const int ft = 128;
+    const size_t factor_smem = sizeof(T) * (size_t)W * ft;
+    if (score_smem > (size_t)smem_optin || factor_smem > (size_t)smem_optin) return -1;
+    // Device state per row of a chunk: the factor, v, z, the gathered
+    // entries, the support, the candidates and five counters; chunks of up
+    // to ~1.5 GB of it.
+    const size_t per_row = sizeof(T) * ((size_t)W * (W + 1) / 2 + 2 * (size_t)W + (size_t)SE * W) +
+                           sizeof(int32_t) * ((size_t)W + SE + 5);
+    const int64_t cap = std::max<int64_t>(4096, (int64_t)(((size_t)1536 << 20) / per_row));
+    const int nc = (int)std::min<int64_t>(n, cap);
+    DevBuf b_size, b_nsel, b_flags, b_pat, b_cand, b_z, b_v, b_L, b_a, b_l0, b_l1, b_count;
+    if ((rc = b_size.alloc(sizeof(int32_t) * nc)) || (rc = b_nsel.alloc(sizeof(int32_t) * nc)) ||
+        (rc = b_flags.alloc(sizeof(int32_t) * nc)) ||
+        (rc = b_pat.alloc(sizeof(int32_t) * (size_t)nc * W)) ||
+        (rc = b_cand.alloc(sizeof(int32_t) * (size_t)nc * SE)) ||
+        (rc = b_z.alloc(sizeof(T) * (size_t)nc * W)) || (rc = b_v.alloc(sizeof(T) * (size_t)nc * W)) ||
+        (rc = b_L.alloc(sizeof(T) * (size_t)nc * W * (W + 1) / 2)) ||
+        (rc = b_a.alloc(sizeof(T) * (size_t)nc * W * SE)) ||
+        (rc = b_l0.alloc(sizeof(int32_t) * nc)) || (rc = b_l1.alloc(sizeof(int32_t) * nc)) ||
+        (rc = b_count.alloc(sizeof(int32_t) * 2)))
+      return rc;
+    RoundState<T> R;
+    R.W = W;
+    R.S = SE;
+    R.H = H;
+    R.hbits = hbits;
+    R.size = b_size.as<int32_t>();
+    R.nsel = b_nsel.as<int32_t>();
+    R.flags = b_flags.as<int32_t>();
+    R.pat = b_pat.as<int32_t>();
+    R.cand = b_cand.as<int32_t>();
+    R.z = b_z.as<T>();
+    R.v = b_v.as<T>();
+    R.L = b_L.as<T>();
+    R.a = b_a.as<T>();
+    R.list0 = b_l0.as<int32_t>();
+    R.list1 = b_l1.as<int32_t>();
+    R.count = b_count.as<int32_t>();
+    GBPC_CUDA_TRY(cudaFuncSetAttribute(fsai_round_score_kernel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)score_smem));
+    GBPC_CUDA_TRY(cudaFuncSetAttribute(fsai_round_factor_kernel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)factor_smem));
+    int sms = 0, occ_s = 0, occ_f = 0;
+    GBPC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GBPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ_s, fsai_round_score_kernel<T>, 32 * wpc, score_smem));
+    GBPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ_f, fsai_round_factor_kernel<T>, ft, factor_smem));
+    const int grid_s = sms * std::max(occ_s, 1), grid_f = sms * std::max(occ_f, 1);
+    for (int r0 = 0; r0 < n; r0 += nc) {
+      R.r0 = r0;
+      R.nc = std::min(nc, n - r0);
+      fsai_round_init_kernel<T><<<grid_for(R.nc, 256), 256, 0, st>>>(R);
+      // Every round adds an entry to each row still growing, or ends it.
+      for (int round = 0; round < W - 1; ++round) {
+        const int cur = round & 1;
+        fsai_round_score_kernel<T><<<grid_s, 32 * wpc, score_smem, st>>>(
+            R, cur, off, col, ahat.as<T>(), ahatT.as<T>(), ovl.as<int32_t>(), stat + 5);
+        fsai_round_factor_kernel<T><<<grid_f, ft, factor_smem, st>>>(R, cur, (T)kap, (T)floor_);
+      }
+      fsai_round_finish_kernel<T><<<grid_for(R.nc, 8), 256, 0, st>>>(R, scale, ell_cols, ell_vals,
+                                                                     counts, stat);
+      GBPC_CUDA_TRY(cudaGetLastError());
+    }
+    return GBPC_OK;
+  };
+  int rr = -1;
+  if (W > 16 && rounds_build_enabled() && (rr = launch_rounds(Hfirst, hbits_first)) > 0)
+    return rr;
+  if (rr == 0) {
+    // built by rounds
+  } else if (W <= 48 && lanes_build_enabled()) {
     if ((rc = launch_lanes(Hfirst, hbits_first))) return rc;
   } else if ((rc = launch(Hfirst, hbits_first, nullptr, n))) {
     return rc;

@@ -214,7 +214,8 @@ class ResidentSystem:
     """Device-resident operator, FSAI factor and Krylov state of one system."""
 
     def __init__(self, host: HostSystem, *, width: int = 8, step: int = 1, kap: float = 1e-3,
-                 max_rhs: int = MAX_RHS, batched: bool = True, device="cuda"):
+                 max_rhs: int = MAX_RHS, batched: bool = True, cluster_rhs: bool = True,
+                 device="cuda"):
         from .batched import BatchedCG, batched_fsai, batched_sparse, batched_sqlap
         from .fsai import FSAI
         from .linear import Solver, aslinearoperator
@@ -249,7 +250,7 @@ class ResidentSystem:
         self.X = torch.zeros(n * max_rhs, dtype=torch.float64, device=dev)
         self.bcg = None
         self.csolver = None
-        if batched and max_rhs > 1 and self.solver.cluster_size > 0:
+        if batched and cluster_rhs and max_rhs > 1 and self.solver.cluster_size > 0:
             # A small system: its single-vector solve runs on one thread-block
             # cluster, so the k right-hand sides of a request run as k such
             # solves in one launch, each the single-vector result bit for bit.
@@ -377,7 +378,8 @@ class GpuExecutor:
 
     def __init__(self, catalog: Catalog, *, slots: int = 16, sequential: bool = False,
                  tol: float = 1e-8, maxiter: int = 0, width: int = 8, step: int = 1,
-                 kap: float = 1e-3, max_rhs: int = MAX_RHS, merge_rhs: int = 0, device="cuda"):
+                 kap: float = 1e-3, max_rhs: int = MAX_RHS, merge_rhs: int = 0,
+                 cluster_rhs: bool = True, device="cuda"):
         if not torch.cuda.is_available():
             raise RuntimeError("GpuExecutor needs a CUDA device")
         if merge_rhs and not 2 <= merge_rhs <= 32:
@@ -391,6 +393,9 @@ class GpuExecutor:
         # to merge_rhs right-hand sides (0: one request per solve).
         self.merge_rhs = 0 if sequential else int(merge_rhs)
         self.max_rhs = max(max_rhs, self.merge_rhs)
+        # Small systems run a request's k right-hand sides as k cluster solves
+        # in one launch (False: the batched solver, as for large systems).
+        self.cluster_rhs = bool(cluster_rhs)
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(self.slots)]
 
@@ -406,7 +411,7 @@ class GpuExecutor:
         m0, l0 = torch.cuda.memory_allocated(self.device), _lib.live_device_bytes()
         res = ResidentSystem(host, width=self.width, step=self.step, kap=self.kap,
                              max_rhs=self.max_rhs, batched=not self.sequential,
-                             device=self.device)
+                             cluster_rhs=self.cluster_rhs, device=self.device)
         res.warm(self.tol)
         cur.synchronize()
         nbytes = (torch.cuda.memory_allocated(self.device) - m0) + (_lib.live_device_bytes() - l0)
