@@ -467,7 +467,7 @@ def main():
                                            solve_total_s, fp64_peak),
         "fp64_peak": fp64_peak,
         "apply_gbps": apply,
-        "gpu_launches": launch_count(iters),
+        "gpu_launches": launch_count(iters, args.width),
     }
     clk = clocks.summary()
     line["clocks"] = clk
@@ -480,6 +480,7 @@ def main():
         line["f32_apply_rhs4"] = measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev,
                                                         ms_per_step)
     if not args.no_mixed:
+        line["wide_fsai"] = measure_wide_fsai(args, prob, Q, K, mass, free, dev, ms_per_step)
         line["multi_system"] = measure_multi_system(dev)
         line["multi_system_small"] = measure_multi_system(dev, sides=(17, 18, 19, 20) * 8)
     line["refit"] = measure_refit(args, prob, Q, dev)
@@ -712,10 +713,12 @@ def _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step, pre_kw, solver
     b = torch.empty(n, dtype=torch.float64, device=dev)
     xs = torch.zeros((4, n), dtype=torch.float64, device=dev)
 
+    kw = dict(max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+    kw.update(pre_kw)
+
     def step():
         op = SquaredLaplacianOperator(K, mass, free, mass_weight=ALPHA)
-        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
-                   kap_tolerance=1e-3, **pre_kw)
+        pre = FSAI(Q, **kw)
         solver = linear.Solver(args.method, op, pre, **solver_kw)
         its = []
         for j in range(4):
@@ -742,8 +745,30 @@ def _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step, pre_kw, solver
     berr = [float(np.max(np.abs(prob["rhs"][j] - qh @ sols[j])
                          / (absq @ np.abs(sols[j]) + np.abs(prob["rhs"][j]))))
             for j in range(4)]
+    setups = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        FSAI(Q, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        setups.append(e0.elapsed_time(e1))
     return {"ms_per_step": t, "solves_per_s": 4e3 / t, "speedup_vs_drop_in": ms_per_step / t,
+            "setup_ms": statistics.median(setups),
             "iterations": [int(i.item()) for i in its], "backward_error_max": max(berr)}
+
+
+def measure_wide_fsai(args, prob, Q, K, mass, free, dev, ms_per_step):
+    """The default step with the wide factors the reference's sweep uses
+    (width 48, steps 1 and 2): fewer CG iterations for a longer setup."""
+    out = {}
+    for step in (1, 2):
+        out[f"w48_step{step}"] = _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step,
+                                               dict(max_row_size=48, max_step_size=step), {})
+    out["solver"] = ("the default step (FSAI setup + 4 sequential CG solves) with "
+                     "FSAI(Q, max_row_size=48, max_step_size=1 or 2, kap_tolerance=1e-3)")
+    return out
 
 
 def measure_f32_apply_rhs4(args, prob, Q, K, mass, free, dev, ms_per_step):
@@ -1379,12 +1404,12 @@ def run_c5(args, dev):
         "server_stats": srv.stats, "clocks": clocks, **out}
 
 
-def launch_count(iters):
+def launch_count(iters, width=8):
     """Kernels of ours launched per timed step, times steps (structure of the code):
     setup = sqlap (index, mass, gather, boundary map, 3 x SELL build of 2 kernels + scan)
-    + FSAI (diag, prep, build, scan 3, pack, transpose 6, 2 x SELL build 3) ;
-    solve = init 7 + 6 per CG iteration."""
-    setup = 4 + 3 * 3 + 3 + 3 + 1 + 6 + 2 * 3
+    + FSAI (diag, prep, build by rounds: init, 2 per round x (width - 1), finish;
+    scan 3, pack, transpose 6, 2 x SELL build 3) ; solve = init 7 + 6 per CG iteration."""
+    setup = 4 + 3 * 3 + (2 + 2 + 2 * (width - 1)) + 3 + 1 + 6 + 2 * 3
     return sum(setup + sum(7 + 6 * i for i in step) for step in iters)
 
 

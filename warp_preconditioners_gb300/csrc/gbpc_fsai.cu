@@ -1,4 +1,9 @@
-// Adaptive FSAI setup on GB300: one warp per factor row.
+// Adaptive FSAI setup on GB300.
+//
+// Two builds of the same rows: by rounds (every row's growth steps in
+// lock step, a scoring launch and a factor launch per step; the default),
+// and one warp per row through all its steps (rows whose candidate table
+// overflows in the first, and every row with GBPC_FSAI_ROUNDS=0).
 //
 // Follows warp_preconditioners/fsai.py:44-176 operation for operation so that
 // the selected supports and the factor values are bit-identical to a
@@ -17,9 +22,9 @@
 //   * the top-`step` selection is a warp-wide arg-max on the IEEE bit pattern
 //     of |residual| (non-negative doubles order like their bit patterns), with
 //     the reference's tie-break (higher score, then lower column);
-//   * the bordered Cholesky forward solve runs column-oriented across lanes,
-//     which performs the same subtraction sequence per entry as the
-//     reference's row-oriented loop.
+//   * the warp-per-row bordered Cholesky forward solve runs column-oriented
+//     across lanes, which performs the same subtraction sequence per entry
+//     as the reference's row-oriented loop.
 // The transpose-position lookup needs a structurally symmetric matrix (any
 // SPD input assembled by summation is); other inputs are rejected.
 
@@ -405,267 +410,8 @@ fsai_build_kernel(BuildParams P, const int32_t* __restrict__ off, const int32_t*
 }
 
 // ---------------------------------------------------------------------------
-// The same build for widths <= 48 with lanes = rows: a warp owns 32
-// consecutive rows.  Candidate scoring and selection stay cooperative, one
-// row at a time (every lane on a slice of that row's frontier, as above),
-// but the bordered factorisation, the substitution L^T z = v and the stop
-// tests of all 32 rows then run at once, lane r on row r, with the same
-// operations in the same order as the warp-per-row kernel.  On this GPU an
-// FP64 warp instruction costs the same however many lanes are active; in
-// the warp-per-row kernel those sequential steps ran on one lane and were
-// ~90% of its FP64 instructions.  Rows whose frontier overflows the
-// candidate table are handed to the warp-per-row rerun like there.
-
-constexpr int kLanesWarps = 4;
-
-__host__ __device__ constexpr size_t lanes_smem_bytes(int T_size, int W, int SC, int H, int PH) {
-  return ((size_t)T_size * ((size_t)H + 32 * (size_t)W) +
-          sizeof(int) * ((size_t)H + 32 * (size_t)W + 32 * (size_t)SC + (size_t)PH) + 15) &
-         ~(size_t)15;
-}
-
-// Membership set of the row being scored: open addressing on the column.
-__device__ __forceinline__ bool pset_has(const int* pkey, int pmask, int pbits, int c) {
-  unsigned int s = hash_col(c) >> (32 - pbits);
-  for (int probe = 0; probe <= pmask; ++probe) {
-    const int k = pkey[s];
-    if (k == c) return true;
-    if (k == kEmpty) return false;
-    s = (s + 1) & pmask;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void pset_add(int* pkey, int pmask, int pbits, int c) {
-  unsigned int s = hash_col(c) >> (32 - pbits);
-  for (int probe = 0; probe <= pmask; ++probe) {
-    if (pkey[s] == kEmpty) {
-      pkey[s] = c;
-      return;
-    }
-    s = (s + 1) & pmask;
-  }
-}
-
-template <typename T, int WMAX>
-__global__ void __launch_bounds__(32 * kLanesWarps)
-fsai_build_lanes_kernel(BuildParams P, const int32_t* __restrict__ off,
-                        const int32_t* __restrict__ col, const T* __restrict__ ahat,
-                        const T* __restrict__ ahatT, const T* __restrict__ scale, T tolerance,
-                        T pivot_floor, int32_t* ell_cols, T* ell_vals, int32_t* row_counts,
-                        int32_t* status) {
-  extern __shared__ __align__(16) unsigned char lanes_smem[];
-  using BitsT = Bits<T>;
-  using U = typename BitsT::U;
-  const int W = P.width, H = P.hsize;
-  const int SC = min(P.step, W);  // candidates ever used per round
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t row0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * 32;
-  if (row0 >= P.n) return;
-  const int PH = P.psize, pmask = PH - 1;
-  unsigned char* base =
-      lanes_smem + (size_t)warp * lanes_smem_bytes((int)sizeof(T), W, SC, H, PH);
-  T* hacc = reinterpret_cast<T*>(base);  // [H]
-  T* zS = hacc + H;                      // [32][W]
-  int* hkey = reinterpret_cast<int*>(zS + 32 * W);  // [H]
-  int* patS = hkey + H;                  // [32][W]
-  int* candS = patS + 32 * W;            // [32][SC]
-  int* pkey = candS + 32 * SC;           // [PH]: support of the row being scored
-  const int hmask = H - 1;
-  const int i = (int)row0 + lane;
-  const bool exists = i < P.n;
-  T* z = zS + lane * W;
-  int* pat = patS + lane * W;
-  // Packed lower triangle by columns, as in the warp-per-row kernel.
-  T Lp[WMAX * (WMAX + 1) / 2];
-  T v[WMAX], a[WMAX], wv[WMAX];
-  auto L = [&](int r, int p) -> T& { return Lp[p * W - (p * (p - 1)) / 2 + (r - p)]; };
-  int size = 1, nsel = 0;
-  bool active = exists, stopped = false, truncated = false, overflowed = false;
-  if (exists) {
-    pat[0] = i;
-    z[0] = T(1);
-    L(0, 0) = T(1);
-    v[0] = T(1);
-  }
-  __syncwarp();
-  while (true) {
-    const bool grow = active && !overflowed && size < W;
-    const unsigned mask = __ballot_sync(0xffffffffu, grow);
-    if (mask == 0u) break;
-    // Scoring and selection, one growing row at a time.
-    for (int r = 0; r < 32; ++r) {
-      if (!((mask >> r) & 1u)) continue;
-      const int rsize = __shfl_sync(0xffffffffu, size, r);
-      const int ri = (int)row0 + r;
-      const int* rpat = patS + r * W;
-      const T* rz = zS + r * W;
-      for (int s2 = lane; s2 < H; s2 += 32) {
-        hkey[s2] = kEmpty;
-        hacc[s2] = T(0);
-      }
-      for (int s2 = lane; s2 < PH; s2 += 32) pkey[s2] = kEmpty;
-      __syncwarp();
-      if (lane == 0)
-        for (int t = 0; t < rsize; ++t) pset_add(pkey, pmask, P.pbits, rpat[t]);
-      __syncwarp();
-      bool overflow = false;
-      for (int q = 0; q < rsize; ++q) {
-        const int pq = rpat[q];
-        const T zq = rz[q];
-        const int e_end = off[pq + 1];
-        for (int e = off[pq] + lane; e < e_end; e += 32) {
-          const int c = col[e];
-          if (c >= ri) continue;
-          if (pset_has(pkey, pmask, P.pbits, c)) continue;
-          const int slot = hfind_insert(hkey, hmask, P.hbits, c);
-          if (slot < 0) {
-            overflow = true;
-          } else {
-            const T t = ahatT[e] * zq;
-            hacc[slot] = hacc[slot] + t;
-          }
-        }
-        __syncwarp();
-      }
-      if (__any_sync(0xffffffffu, overflow)) {
-        if (lane == r) overflowed = true;
-        continue;
-      }
-      // Top candidates: higher score, then lower column (as above).
-      const int want = min(SC, W - rsize);
-      int ns = 0;
-      for (int k = 0; k < want; ++k) {
-        U best_bits = 0;
-        int best_col = 0x7fffffff;
-        int best_slot = -1;
-        for (int s2 = lane; s2 < H; s2 += 32) {
-          const int kk = hkey[s2];
-          if (kk < 0) continue;
-          const U bits = BitsT::abs_bits(hacc[s2]);
-          if (bits == 0 || bits > BitsT::kInf) continue;
-          if (bits > best_bits || (bits == best_bits && kk < best_col)) {
-            best_bits = bits;
-            best_col = kk;
-            best_slot = s2;
-          }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const U ob = __shfl_xor_sync(0xffffffffu, best_bits, o);
-          const int oc = __shfl_xor_sync(0xffffffffu, best_col, o);
-          const int os = __shfl_xor_sync(0xffffffffu, best_slot, o);
-          if (ob > best_bits || (ob == best_bits && oc < best_col)) {
-            best_bits = ob;
-            best_col = oc;
-            best_slot = os;
-          }
-        }
-        if (best_slot < 0) break;
-        if (lane == 0) {
-          candS[r * SC + k] = best_col;
-          hkey[best_slot] = kTomb;
-        }
-        __syncwarp();
-        ++ns;
-      }
-      if (lane == r) nsel = ns;
-    }
-    __syncwarp();
-    // Factor updates of every growing row at once.
-    if (grow && !overflowed) {
-      if (nsel == 0) {
-        active = false;
-      } else {
-        const T old_z0 = z[0];
-        for (int k = 0; k < nsel; ++k) {
-          if (size == W) break;
-          const int best = candS[lane * SC + k];
-          const int b0 = off[best], b1 = off[best + 1];
-          for (int p = 0; p < size; ++p) {
-            const int pc = pat[p];
-            const int lo = lower_bound_row(col, b0, b1, pc);
-            a[p] = (lo < b1 && col[lo] == pc) ? ahat[lo] : T(0);
-          }
-          T pivot = T(1);
-          T rhs = T(0);
-          for (int p = 0; p < size; ++p) {
-            const T wp = a[p] / L(p, p);
-            wv[p] = wp;
-            const T sq = wp * wp;
-            pivot = pivot - sq;
-            const T pr = wp * v[p];
-            rhs = rhs - pr;
-            for (int l = p + 1; l < size; ++l) {
-              const T t = L(l, p) * wp;
-              a[l] = a[l] - t;
-            }
-          }
-          if (pivot <= pivot_floor || !isfinite(pivot)) {
-            truncated = true;
-            stopped = true;
-            break;
-          }
-          for (int p = 0; p < size; ++p) L(size, p) = wv[p];
-          pat[size] = best;
-          const T d = sqrt(pivot);
-          L(size, size) = d;
-          v[size] = rhs / d;
-          ++size;
-        }
-        // L^T z = v, in the reference's order.
-        for (int p = size - 1; p >= 0; --p) {
-          T acc = v[p];
-          for (int q = p + 1; q < size; ++q) {
-            const T t = L(q, p) * z[q];
-            acc = acc - t;
-          }
-          z[p] = acc / L(p, p);
-        }
-        if (stopped) {
-          active = false;
-        } else if (tolerance > T(0)) {
-          const T ratio = old_z0 / z[0];
-          if (T(1) - ratio <= tolerance) active = false;
-        }
-      }
-    }
-    __syncwarp();
-  }
-  if (!exists) return;
-  if (overflowed) {
-    const int k = atomicAdd(P.overflow_count, 1);
-    P.overflow_list[k] = i;
-    return;
-  }
-  // Normalise, validate, sort by column, write the ELL row.
-  const T norm = sqrt(z[0]);
-  bool valid = true;
-  int32_t* oc = ell_cols + (size_t)i * W;
-  T* ov = ell_vals + (size_t)i * W;
-  for (int p = 0; p < size; ++p) {
-    const int c = pat[p];
-    const T t = z[p] / norm;
-    const T val = t * scale[c];
-    if (!isfinite(val)) valid = false;
-    if (p == 0 && !(val > T(0))) valid = false;
-    int rank = 0;
-    for (int q = 0; q < size; ++q) rank += (pat[q] < c);
-    oc[rank] = c;
-    ov[rank] = val;
-  }
-  for (int p = size; p < W; ++p) {
-    oc[p] = -1;
-    ov[p] = T(0);
-  }
-  row_counts[i] = size;
-  if (truncated) atomicAdd(status + 1, 1);
-  if (!valid) atomicAdd(status + 2, 1);
-}
-
-// ---------------------------------------------------------------------------
-// Wide rows (W > 16) by rounds.  A round is one growth step of every row
-// still growing, in two launches:
+// The build by rounds.  A round is one growth step of every row still
+// growing, in two launches:
 //   * scoring, a warp per row: the row's support goes into a shared-memory
 //     hash table (marked with its position), the frontier's residuals are
 //     summed in support order as above, the step's candidates are selected,
@@ -694,6 +440,7 @@ struct RoundState {
   int32_t* nsel;    // [nc] candidates selected this round
   int32_t* flags;   // [nc] bit 0: truncated; bit 1: table overflow
   int32_t* pat;     // [nc][W] support in insertion order
+  int32_t* lo;      // [nc][W] end of the entries of row pat[p] in columns < the row
   int32_t* cand;    // [nc][S]
   T* z;             // [nc][W]
   T* v;             // [W][nc]
@@ -705,11 +452,12 @@ struct RoundState {
 };
 
 __host__ __device__ constexpr size_t round_smem_per_warp(int T_size, int H) {
-  return ((size_t)H * (T_size + sizeof(int) + 1) + 15) & ~(size_t)15;
+  return ((size_t)H * (T_size + sizeof(int) + sizeof(unsigned short) + 1) + 15) & ~(size_t)15;
 }
 
 template <typename T>
-__global__ void fsai_round_init_kernel(RoundState<T> R) {
+__global__ void fsai_round_init_kernel(RoundState<T> R, const int32_t* __restrict__ off,
+                                       const int32_t* __restrict__ col) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j == 0) {
     R.count[0] = R.nc;
@@ -721,6 +469,7 @@ __global__ void fsai_round_init_kernel(RoundState<T> R) {
   R.nsel[j] = 0;
   R.flags[j] = 0;
   R.pat[(size_t)j * R.W] = i;
+  R.lo[(size_t)j * R.W] = lower_bound_row(col, off[i], off[i + 1], i);
   R.z[(size_t)j * R.W] = T(1);
   R.v[j] = T(1);
   R.L[j] = T(1);
@@ -759,8 +508,28 @@ __device__ __forceinline__ int hfind(const int* hkey, int hmask, int hbits, int 
   return -1;
 }
 
+// Per-warp scoring table: residuals, columns, the marks below and the list
+// of occupied slots (so that selection and clearing visit only those).
 template <typename T>
-__global__ void __launch_bounds__(256)
+struct ScoreTable {
+  T* acc;
+  int* key;
+  signed char* pos;  // 0 a candidate; p + 1 the support column at position p;
+                     // -(k + 1) the k-th candidate selected this round
+  unsigned short* used;
+  int nused;         // the same in every lane
+  int mask, bits;
+
+  // Note slot s, newly taken by the lanes whose `fresh` is set.
+  __device__ __forceinline__ void note(bool fresh, int s, int lane) {
+    const unsigned m = __ballot_sync(0xffffffffu, fresh);
+    if (fresh) used[nused + __popc(m & ((1u << lane) - 1u))] = (unsigned short)s;
+    nused += __popc(m);
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128)
 fsai_round_score_kernel(RoundState<T> R, int cur, const int32_t* __restrict__ off,
                         const int32_t* __restrict__ col, const T* __restrict__ ahat,
                         const T* __restrict__ ahatT, int32_t* overflow_list,
@@ -769,17 +538,22 @@ fsai_round_score_kernel(RoundState<T> R, int cur, const int32_t* __restrict__ of
   using BitsT = Bits<T>;
   using U = typename BitsT::U;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int W = R.W, S = R.S, H = R.H, hbits = R.hbits, hmask = H - 1;
+  const int W = R.W, S = R.S, H = R.H;
   const int64_t nc = R.nc;
   unsigned char* base = round_smem + (size_t)warp * round_smem_per_warp((int)sizeof(T), H);
-  T* hacc = reinterpret_cast<T*>(base);                    // [H] residuals
-  int* hkey = reinterpret_cast<int*>(hacc + H);            // [H] columns
-  signed char* hpos = reinterpret_cast<signed char*>(hkey + H);  // [H] see below
-  // hpos: 0 a candidate; p + 1 the support column at position p; -(k + 1)
-  // the k-th candidate selected this round.
+  ScoreTable<T> tb;
+  tb.acc = reinterpret_cast<T*>(base);
+  tb.key = reinterpret_cast<int*>(tb.acc + H);
+  tb.used = reinterpret_cast<unsigned short*>(tb.key + H);
+  tb.pos = reinterpret_cast<signed char*>(tb.used + H);
+  tb.nused = 0;
+  tb.mask = H - 1;
+  tb.bits = R.hbits;
   if (blockIdx.x == 0 && threadIdx.x == 0) R.count[cur ^ 1] = 0;
   const int count = R.count[cur];
   const int32_t* list = cur ? R.list1 : R.list0;
+  for (int s = lane; s < H; s += 32) tb.key[s] = kEmpty;
+  __syncwarp();
   for (int idx = blockIdx.x * nw + warp; idx < count; idx += gridDim.x * nw) {
     const int j = list[idx];
     const int i = R.r0 + j;
@@ -797,108 +571,149 @@ fsai_round_score_kernel(RoundState<T> R, int cur, const int32_t* __restrict__ of
         pc[h] = R.pat[(size_t)j * W + p];
         zv[h] = R.z[(size_t)j * W + p];
         ob[h] = off[pc[h]];
-        oe[h] = off[pc[h] + 1];
+        oe[h] = R.lo[(size_t)j * W + p];  // rows are sorted: columns < i come first
       }
     }
-    for (int s = lane; s < H; s += 32) hkey[s] = kEmpty;
-    __syncwarp();
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
+      bool fresh = false;
+      int s = -1;
       if (pc[h] >= 0) {
-        bool fresh;
-        const int s = hfind_insert_fresh(hkey, hmask, hbits, pc[h], fresh);
-        if (s >= 0) hpos[s] = (signed char)(lane + 32 * h + 1);  // H > W: always found
+        s = hfind_insert_fresh(tb.key, tb.mask, tb.bits, pc[h], fresh);
+        if (s >= 0) tb.pos[s] = (signed char)(lane + 32 * h + 1);  // H > W: always found
       }
+      tb.note(fresh, s, lane);
     }
     __syncwarp();
-    // Frontier residuals, summed in support order.
+    // Frontier residuals, summed in support order.  Only the entries of a
+    // support row in columns < i can score; the work is a sequence of
+    // (support position, 32 of those entries) items, and the next item's
+    // entries are loaded before the current one is summed.
     bool overflow = false;
-    for (int q = 0; q < size; ++q) {
+    auto item_row = [&](int q, int& b, int& e, T& zq) {
       const int h = q >> 5, src = q & 31;
-      const int b = __shfl_sync(0xffffffffu, h ? ob[1] : ob[0], src);
-      const int e_end = __shfl_sync(0xffffffffu, h ? oe[1] : oe[0], src);
-      const T zq = __shfl_sync(0xffffffffu, h ? zv[1] : zv[0], src);
-      for (int e = b + lane; e < e_end; e += 32) {
-        const int c = col[e];
-        if (c >= i) continue;
-        bool fresh;
-        const int s = hfind_insert_fresh(hkey, hmask, hbits, c, fresh);
+      b = __shfl_sync(0xffffffffu, h ? ob[1] : ob[0], src);
+      e = __shfl_sync(0xffffffffu, h ? oe[1] : oe[0], src);
+      zq = __shfl_sync(0xffffffffu, h ? zv[1] : zv[0], src);
+    };
+    int q = 0, e0, qe;
+    T zq;
+    item_row(0, e0, qe, zq);
+    int cc = -1;
+    T tt = T(0);
+    if (e0 + lane < qe) {
+      cc = col[e0 + lane];
+      tt = ahatT[e0 + lane];
+    }
+    while (q < size) {
+      int nq = q, ne0 = e0 + 32, nqe = qe;
+      T nzq = zq;
+      if (ne0 >= qe) {
+        nq = q + 1;
+        if (nq < size) item_row(nq, ne0, nqe, nzq);
+      }
+      int ncc = -1;
+      T ntt = T(0);
+      if (nq < size && ne0 + lane < nqe) {
+        ncc = col[ne0 + lane];
+        ntt = ahatT[ne0 + lane];
+      }
+      bool fresh = false;
+      int s = -1;
+      if (cc >= 0) {
+        const T t = tt * zq;
+        s = hfind_insert_fresh(tb.key, tb.mask, tb.bits, cc, fresh);
         if (s < 0) {
           overflow = true;
         } else if (fresh) {
-          hpos[s] = 0;
-          hacc[s] = ahatT[e] * zq;  // 0 + t: the same magnitude, which is all the score reads
-        } else if (hpos[s] == 0) {
-          const T t = ahatT[e] * zq;
-          hacc[s] = hacc[s] + t;
+          tb.pos[s] = 0;
+          tb.acc[s] = t;  // 0 + t: the same magnitude, all the score reads
+        } else if (tb.pos[s] == 0) {
+          tb.acc[s] = tb.acc[s] + t;
         }
       }
+      tb.note(fresh, s, lane);
       __syncwarp();
+      q = nq;
+      e0 = ne0;
+      qe = nqe;
+      zq = nzq;
+      cc = ncc;
+      tt = ntt;
     }
+    int ns = 0;
     if (__any_sync(0xffffffffu, overflow)) {
       if (lane == 0) {
         R.flags[j] |= 2;
-        R.nsel[j] = 0;
         overflow_list[atomicAdd(overflow_count, 1)] = i;
       }
-      continue;
-    }
-    // Top candidates: higher score, then lower column.
-    const int want = min(S, W - size);
-    int ns = 0;
-    for (int k = 0; k < want; ++k) {
-      U best_bits = 0;
-      int best_col = 0x7fffffff;
-      int best_slot = -1;
-      for (int s = lane; s < H; s += 32) {
-        const int kk = hkey[s];
-        if (kk < 0 || hpos[s] != 0) continue;
-        const U bits = BitsT::abs_bits(hacc[s]);
-        if (bits == 0 || bits > BitsT::kInf) continue;  // zero or NaN: never selected
-        if (bits > best_bits || (bits == best_bits && kk < best_col)) {
-          best_bits = bits;
-          best_col = kk;
-          best_slot = s;
+    } else {
+      // Top candidates: higher score, then lower column.
+      const int want = min(S, W - size);
+      for (int k = 0; k < want; ++k) {
+        U best_bits = 0;
+        int best_col = 0x7fffffff;
+        int best_slot = -1;
+        for (int t = lane; t < tb.nused; t += 32) {
+          const int s = tb.used[t];
+          if (tb.pos[s] != 0) continue;
+          const int kk = tb.key[s];
+          const U bits = BitsT::abs_bits(tb.acc[s]);
+          if (bits == 0 || bits > BitsT::kInf) continue;  // zero or NaN: never selected
+          if (bits > best_bits || (bits == best_bits && kk < best_col)) {
+            best_bits = bits;
+            best_col = kk;
+            best_slot = s;
+          }
         }
-      }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const U ob2 = __shfl_xor_sync(0xffffffffu, best_bits, o);
-        const int oc = __shfl_xor_sync(0xffffffffu, best_col, o);
-        const int os = __shfl_xor_sync(0xffffffffu, best_slot, o);
-        if (ob2 > best_bits || (ob2 == best_bits && oc < best_col)) {
-          best_bits = ob2;
-          best_col = oc;
-          best_slot = os;
+        for (int o = 16; o > 0; o >>= 1) {
+          const U ob2 = __shfl_xor_sync(0xffffffffu, best_bits, o);
+          const int oc = __shfl_xor_sync(0xffffffffu, best_col, o);
+          const int os = __shfl_xor_sync(0xffffffffu, best_slot, o);
+          if (ob2 > best_bits || (ob2 == best_bits && oc < best_col)) {
+            best_bits = ob2;
+            best_col = oc;
+            best_slot = os;
+          }
         }
+        if (best_slot < 0) break;
+        if (lane == 0) {
+          tb.pos[best_slot] = (signed char)(-(k + 1));
+          R.cand[(size_t)j * S + k] = best_col;
+        }
+        __syncwarp();
+        ++ns;
       }
-      if (best_slot < 0) break;
-      if (lane == 0) {
-        hpos[best_slot] = (signed char)(-(k + 1));
-        R.cand[(size_t)j * S + k] = best_col;
-      }
+      // Entries of each candidate against the support and the candidates
+      // selected before it; zero where the matrix stores none.
+      for (int k = 0; k < ns; ++k)
+        for (int p = lane; p < size + k; p += 32) R.a[((size_t)k * W + p) * nc + j] = T(0);
       __syncwarp();
-      ++ns;
-    }
-    // Entries of each candidate against the support and the candidates
-    // selected before it; zero where the matrix stores none.
-    for (int k = 0; k < ns; ++k)
-      for (int p = lane; p < size + k; p += 32) R.a[((size_t)k * W + p) * nc + j] = T(0);
-    __syncwarp();
-    for (int k = 0; k < ns; ++k) {
-      const int best = R.cand[(size_t)j * S + k];
-      const int e_end = off[best + 1];
-      for (int e = off[best] + lane; e < e_end; e += 32) {
-        const int s = hfind(hkey, hmask, hbits, col[e]);
-        if (s < 0) continue;
-        const int hp = hpos[s];
-        int pos = -1;
-        if (hp > 0) pos = hp - 1;
-        else if (hp < 0 && -hp - 1 < k) pos = size + (-hp - 1);
-        if (pos >= 0) R.a[((size_t)k * W + pos) * nc + j] = ahat[e];
+      for (int k = 0; k < ns; ++k) {
+        const int best = R.cand[(size_t)j * S + k];
+        const int e_beg = off[best], e_end = off[best + 1];
+        int below = 0;  // entries of the candidate's row in columns < i
+        for (int e0 = e_beg; e0 < e_end; e0 += 32) {
+          const int e = e0 + lane;
+          const int c = e < e_end ? col[e] : 0x7fffffff;
+          below += __popc(__ballot_sync(0xffffffffu, c < i));
+          const int s = e < e_end ? hfind(tb.key, tb.mask, tb.bits, c) : -1;
+          if (s < 0) continue;
+          const int hp = tb.pos[s];
+          int pos = -1;
+          if (hp > 0) pos = hp - 1;
+          else if (hp < 0 && -hp - 1 < k) pos = size + (-hp - 1);
+          if (pos >= 0) R.a[((size_t)k * W + pos) * nc + j] = ahat[e];
+        }
+        if (lane == 0) R.lo[(size_t)j * W + size + k] = e_beg + below;
       }
     }
     if (lane == 0) R.nsel[j] = ns;
+    // Empty the slots this row used.
+    __syncwarp();
+    for (int t = lane; t < tb.nused; t += 32) tb.key[tb.used[t]] = kEmpty;
+    tb.nused = 0;
     __syncwarp();
   }
 }
@@ -936,11 +751,25 @@ fsai_round_factor_kernel(RoundState<T> R, int cur, T tolerance, T pivot_floor) {
           T rhs = T(0);
           for (int p = 0; p < size; ++p) {
             T acc = ak[(size_t)p * nc];
-            for (int q = 0; q < p; ++q) {
-              const T t = L(p, q) * w[q * nt];
+            const T* Lrow = Lj + (size_t)(p * (p + 1) / 2) * nc;  // L(p, q) at Lrow[q nc]
+            const T dp = Lrow[(size_t)p * nc];
+            int q = 0;
+            // Loads in batches of 8 ahead of the (sequential) subtractions.
+            for (; q + 8 <= p; q += 8) {
+              T l[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) l[u] = Lrow[(size_t)(q + u) * nc];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) {
+                const T t = l[u] * w[(q + u) * nt];
+                acc = acc - t;
+              }
+            }
+            for (; q < p; ++q) {
+              const T t = Lrow[(size_t)q * nc] * w[q * nt];
               acc = acc - t;
             }
-            const T wp = acc / L(p, p);
+            const T wp = acc / dp;
             w[p * nt] = wp;
             const T sq = wp * wp;
             pivot = pivot - sq;
@@ -961,11 +790,30 @@ fsai_round_factor_kernel(RoundState<T> R, int cur, T tolerance, T pivot_floor) {
         // L^T z = v, in the reference's order.
         for (int p = size - 1; p >= 0; --p) {
           T acc = vj[(size_t)p * nc];
-          for (int q = p + 1; q < size; ++q) {
-            const T t = L(q, p) * w[q * nt];
-            acc = acc - t;
+          const T dp = L(p, p);
+          int q = p + 1;
+          int k0 = q * (q + 1) / 2 + p;  // packed index of L(q, p)
+          for (; q + 8 <= size; q += 8) {
+            T l[8];
+            int kk = k0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              l[u] = Lj[(size_t)kk * nc];
+              kk += q + u + 1;
+            }
+            k0 = kk;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const T t = l[u] * w[(q + u) * nt];
+              acc = acc - t;
+            }
           }
-          w[p * nt] = acc / L(p, p);
+          for (; q < size; ++q) {
+            const T t = Lj[(size_t)k0 * nc] * w[q * nt];
+            acc = acc - t;
+            k0 += q + 1;
+          }
+          w[p * nt] = acc / dp;
         }
         for (int p = 0; p < size; ++p) R.z[(size_t)j * W + p] = w[p * nt];
         R.size[j] = size;
@@ -1422,16 +1270,8 @@ __global__ void scatter_values_kernel(int64_t count, const V* __restrict__ src,
 // ---------------------------------------------------------------------------
 // Host entry points.
 
-// GBPC_FSAI_LANES=0 selects the warp-per-row build for every width (the two
+// GBPC_FSAI_ROUNDS=0 selects the warp-per-row build for every row (the two
 // builds give identical factors; the switch exists to compare them).
-static bool lanes_build_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("GBPC_FSAI_LANES");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
 static bool rounds_build_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("GBPC_FSAI_ROUNDS");
@@ -1521,42 +1361,7 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     GBPC_CUDA_TRY(cudaGetLastError());
     return GBPC_OK;
   };
-  // First pass: lanes = rows for widths <= 48 (see fsai_build_lanes_kernel;
-  // at 48 the per-thread factor, 10.6 KB in float64, lives in local memory).
-  auto launch_lanes = [&](int H, int hbits) -> int {
-    const int SC = std::min(S, W);
-    const size_t per_warp = lanes_smem_bytes((int)sizeof(T), W, SC, H, PH);
-    if (per_warp > (size_t)smem_optin) return launch(H, hbits, nullptr, n);
-    // Warps per CTA: up to kLanesWarps while a CTA stays within ~64 KB, so
-    // that wide rows (whose per-warp tables are large) still get several
-    // resident CTAs per SM instead of one.
-    int wpc = (int)std::min<size_t>(kLanesWarps, std::max<size_t>(1, (64 * 1024) / per_warp));
-    const size_t smem = per_warp * wpc;
-    auto kern = (W <= 8) ? fsai_build_lanes_kernel<T, 8>
-                : (W <= 16) ? fsai_build_lanes_kernel<T, 16> : fsai_build_lanes_kernel<T, 48>;
-    GBPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-    BuildParams P;
-    P.n = n;
-    P.width = W;
-    P.step = S;
-    P.hsize = H;
-    P.hbits = hbits;
-    P.psize = PH;
-    P.pbits = pbits;
-    P.rows = nullptr;
-    P.nrows_list = 0;
-    P.overflow_list = ovl.as<int32_t>();
-    P.overflow_count = stat + 5;
-    const int64_t warps_needed = ((int64_t)n + 31) / 32;
-    if (n > 0)
-      kern<<<(int)((warps_needed + wpc - 1) / wpc), 32 * wpc, smem, st>>>(
-          P, off, col, ahat.as<T>(), ahatT.as<T>(), scale, (T)kap, (T)floor_, ell_cols, ell_vals,
-          counts, stat);
-    GBPC_CUDA_TRY(cudaGetLastError());
-    return GBPC_OK;
-  };
-  // Widths above 16: the build by rounds (see fsai_round_score_kernel).
+  // First pass: the build by rounds (see fsai_round_score_kernel).
   auto launch_rounds = [&](int H, int hbits) -> int {
     const int SE = std::min(S, W);
     const size_t per_warp = round_smem_per_warp((int)sizeof(T), H);
@@ -1566,16 +1371,23 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     const size_t factor_smem = sizeof(T) * (size_t)W * ft;
     if (score_smem > (size_t)smem_optin || factor_smem > (size_t)smem_optin) return -1;
     // Device state per row of a chunk: the factor, v, z, the gathered
-    // entries, the support, the candidates and five counters; chunks of up
-    // to ~1.5 GB of it.
+    // entries, the support and its rows' ends, the candidates and five
+    // counters.
     const size_t per_row = sizeof(T) * ((size_t)W * (W + 1) / 2 + 2 * (size_t)W + (size_t)SE * W) +
-                           sizeof(int32_t) * ((size_t)W + SE + 5);
-    const int64_t cap = std::max<int64_t>(4096, (int64_t)(((size_t)1536 << 20) / per_row));
+                           sizeof(int32_t) * (2 * (size_t)W + SE + 5);
+    // One chunk when the state fits in a quarter of the free memory (8 GB
+    // at most): the last rounds, when few rows still grow, are latency
+    // bound, and each chunk pays them once.
+    size_t free_b = 0, total_b = 0;
+    GBPC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = std::min<size_t>(free_b / 4, (size_t)8 << 30);
+    const int64_t cap = std::max<int64_t>(4096, (int64_t)(budget / per_row));
     const int nc = (int)std::min<int64_t>(n, cap);
-    DevBuf b_size, b_nsel, b_flags, b_pat, b_cand, b_z, b_v, b_L, b_a, b_l0, b_l1, b_count;
+    DevBuf b_size, b_nsel, b_flags, b_pat, b_lo, b_cand, b_z, b_v, b_L, b_a, b_l0, b_l1, b_count;
     if ((rc = b_size.alloc(sizeof(int32_t) * nc)) || (rc = b_nsel.alloc(sizeof(int32_t) * nc)) ||
         (rc = b_flags.alloc(sizeof(int32_t) * nc)) ||
         (rc = b_pat.alloc(sizeof(int32_t) * (size_t)nc * W)) ||
+        (rc = b_lo.alloc(sizeof(int32_t) * (size_t)nc * W)) ||
         (rc = b_cand.alloc(sizeof(int32_t) * (size_t)nc * SE)) ||
         (rc = b_z.alloc(sizeof(T) * (size_t)nc * W)) || (rc = b_v.alloc(sizeof(T) * (size_t)nc * W)) ||
         (rc = b_L.alloc(sizeof(T) * (size_t)nc * W * (W + 1) / 2)) ||
@@ -1592,6 +1404,7 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     R.nsel = b_nsel.as<int32_t>();
     R.flags = b_flags.as<int32_t>();
     R.pat = b_pat.as<int32_t>();
+    R.lo = b_lo.as<int32_t>();
     R.cand = b_cand.as<int32_t>();
     R.z = b_z.as<T>();
     R.v = b_v.as<T>();
@@ -1614,7 +1427,7 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     for (int r0 = 0; r0 < n; r0 += nc) {
       R.r0 = r0;
       R.nc = std::min(nc, n - r0);
-      fsai_round_init_kernel<T><<<grid_for(R.nc, 256), 256, 0, st>>>(R);
+      fsai_round_init_kernel<T><<<grid_for(R.nc, 256), 256, 0, st>>>(R, off, col);
       // Every round adds an entry to each row still growing, or ends it.
       for (int round = 0; round < W - 1; ++round) {
         const int cur = round & 1;
@@ -1629,15 +1442,14 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     return GBPC_OK;
   };
   int rr = -1;
-  if (W > 16 && rounds_build_enabled() && (rr = launch_rounds(Hfirst, hbits_first)) > 0)
-    return rr;
-  if (rr == 0) {
-    // built by rounds
-  } else if (W <= 48 && lanes_build_enabled()) {
-    if ((rc = launch_lanes(Hfirst, hbits_first))) return rc;
-  } else if ((rc = launch(Hfirst, hbits_first, nullptr, n))) {
-    return rc;
-  }
+  // The scoring tables of the build by rounds: 512 slots unless the
+  // longest row makes fewer enough.  (A tet-mesh biharmonic row at width 48
+  // meets ~170 distinct columns, 330 at most; rows that find more rerun
+  // below with a table that cannot overflow.)
+  int Hr = Hfull, hbits_r = hbits_full;
+  while (Hr > 512) { Hr >>= 1; --hbits_r; }
+  if (rounds_build_enabled() && (rr = launch_rounds(Hr, hbits_r)) > 0) return rr;
+  if (rr != 0 && (rc = launch(Hfirst, hbits_first, nullptr, n))) return rc;
   GBPC_CUDA_TRY(cudaMemcpyAsync(h, stat, sizeof(h), cudaMemcpyDeviceToHost, st));
   GBPC_CUDA_TRY(cudaStreamSynchronize(st));
   if (h[5] > 0) {
