@@ -78,7 +78,7 @@ def test_refit_local_solves_and_rollback(block, dtype, step):
 @pytest.mark.parametrize("mdt,fdt", [(torch.float64, torch.float64),
                                      (torch.float64, torch.float32),
                                      (torch.float32, torch.float32)])
-@pytest.mark.parametrize("width,step", [(8, 1), (8, 2), (12, 2), (24, 3)])
+@pytest.mark.parametrize("width,step", [(8, 1), (8, 2), (12, 2), (24, 3), (48, 1)])
 def test_refit_bit_exact_against_oracle(oracle, mdt, fdt, width, step):
     from warp_preconditioners_gb300 import FSAI, problems
 

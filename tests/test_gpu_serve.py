@@ -36,13 +36,14 @@ def host_matrix(h):
     return h.assembled()  # L, or the assembled alpha M + K M^-1 K
 
 
-def test_alone_equals_mixed(catalog):
+@pytest.mark.parametrize("cluster_rhs", [False, True])
+def test_alone_equals_mixed(catalog, cluster_rhs):
     stream = small_stream()
-    mixed_ex = serve.GpuExecutor(catalog, slots=6, tol=TOL)
+    mixed_ex = serve.GpuExecutor(catalog, slots=6, tol=TOL, cluster_rhs=cluster_rhs)
     mixed = serve.Server(mixed_ex).run(stream)
     assert all(r.ok for r in mixed), [r.error for r in mixed if not r.ok]
     # Each request again, alone, on a fresh executor (fresh systems and slots).
-    alone_ex = serve.GpuExecutor(catalog, slots=1, tol=TOL)
+    alone_ex = serve.GpuExecutor(catalog, slots=1, tol=TOL, cluster_rhs=cluster_rhs)
     for req, m in zip(stream, mixed):
         a = serve.Server(alone_ex).run([serve.Request(req.rid, req.kind, req.side, req.k, 0.0,
                                                       req.seed)])[0]

@@ -1235,6 +1235,123 @@ fsai_refit_row_kernel(int n, const int32_t* __restrict__ a_off, const int32_t* _
   if (!valid) atomicAdd(bad, 1);
 }
 
+// The same refit for wider supports, one thread per row: the local factor
+// lives in device memory as a structure of arrays over the rows of a chunk
+// (L(p, q) of the k-th row at L[(p(p+1)/2 + q) stride + k], so the threads
+// of a warp read consecutive words) and z in shared memory.  Rows are taken
+// in order of support size (`order`), so the threads of a warp run loops of
+// the same length.  A[r, S] is gathered by merging the sorted row r with the
+// sorted support.  Operations and their order are the reference's.
+template <typename T, typename S>
+__global__ void __launch_bounds__(128)
+fsai_refit_wide_kernel(int count, const int32_t* __restrict__ order, int64_t stride, T* L,
+                       const int32_t* __restrict__ a_off, const int32_t* __restrict__ a_col,
+                       const T* __restrict__ a_val, const T* __restrict__ scale,
+                       const int32_t* __restrict__ g_off, const int32_t* __restrict__ g_col,
+                       int W, T floor, S* out, int32_t* bad) {
+  extern __shared__ __align__(16) unsigned char refit_wide_smem[];
+  T* z = reinterpret_cast<T*>(refit_wide_smem) + threadIdx.x;  // z[p] at z[p * blockDim.x]
+  const int nt = blockDim.x;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int i = order[k];
+  const int start = g_off[i];
+  const int size = g_off[i + 1] - start;
+  if (size < 1 || size > W) {
+    atomicAdd(bad, 1);
+    return;
+  }
+  T* Lk = L + k;
+  auto at = [&](int p, int q) -> T& { return Lk[(size_t)(p * (p + 1) / 2 + q) * stride]; };
+  bool valid = true;
+  for (int p = 0; p < size; ++p) {
+    const int r = g_col[start + p];
+    const T sr = scale[r];
+    int e = a_off[r];
+    const int rhi = a_off[r + 1];
+    const T* Lp = Lk + (size_t)(p * (p + 1) / 2) * stride;  // row p: Lp[q stride]
+    for (int q = 0; q <= p; ++q) {
+      const int c = g_col[start + q];
+      while (e < rhi && a_col[e] < c) ++e;
+      T a = T(0);
+      if (e < rhi && a_col[e] == c) a = a_val[e] * sr * scale[c];
+      const T* Lq = Lk + (size_t)(q * (q + 1) / 2) * stride;
+      int t = 0;
+      for (; t + 8 <= q; t += 8) {
+        T x[8], y[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          x[u] = Lp[(size_t)(t + u) * stride];
+          y[u] = Lq[(size_t)(t + u) * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a = a - x[u] * y[u];
+      }
+      for (; t < q; ++t) a = a - Lp[(size_t)t * stride] * Lq[(size_t)t * stride];
+      if (p == q) {
+        if (a <= floor || !isfinite(a)) {
+          valid = false;
+          a = T(1);
+        }
+        at(p, p) = sqrt(a);
+      } else {
+        at(p, q) = a / Lq[(size_t)q * stride];
+      }
+    }
+  }
+  for (int p = 0; p < size; ++p) {
+    T a = (g_col[start + p] == i) ? T(1) : T(0);
+    const T* Lp = Lk + (size_t)(p * (p + 1) / 2) * stride;
+    for (int q = 0; q < p; ++q) a = a - Lp[(size_t)q * stride] * z[q * nt];
+    z[p * nt] = a / Lp[(size_t)p * stride];
+  }
+  for (int p = size - 1; p >= 0; --p) {
+    T a = z[p * nt];
+    int kk = (p + 1) * (p + 2) / 2 + p;  // packed index of L(p + 1, p)
+    for (int q = p + 1; q < size; ++q) {
+      a = a - Lk[(size_t)kk * stride] * z[q * nt];
+      kk += q + 1;
+    }
+    z[p * nt] = a / at(p, p);
+  }
+  const T norm = sqrt(z[(size - 1) * nt]);
+  for (int p = 0; p < size; ++p) {
+    const S v = narrow<T, S>(z[p * nt] / norm * scale[g_col[start + p]]);
+    out[start + p] = v;
+    if (!finite_value(v)) valid = false;
+    if (p == size - 1 && nonpositive(v)) valid = false;
+  }
+  if (!valid) atomicAdd(bad, 1);
+}
+
+// Rows ordered by support size (counting sort; the order within a size is
+// immaterial, every row is computed on its own).
+__global__ void support_size_count_kernel(int n, const int32_t* __restrict__ g_off, int W,
+                                          int32_t* bins) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = min(max(g_off[i + 1] - g_off[i], 0), W);
+  atomicAdd(bins + s, 1);
+}
+
+__global__ void support_size_scan_kernel(int W, int32_t* bins) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int acc = 0;
+  for (int s = 0; s <= W; ++s) {
+    const int c = bins[s];
+    bins[s] = acc;
+    acc += c;
+  }
+}
+
+__global__ void support_size_scatter_kernel(int n, const int32_t* __restrict__ g_off, int W,
+                                            int32_t* cursor, int32_t* order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = min(max(g_off[i + 1] - g_off[i], 0), W);
+  order[atomicAdd(cursor + s, 1)] = i;
+}
+
 // map[e] = position of entry (i, j) of a CSR matrix in its transpose's row j.
 __global__ void transpose_map_kernel(int nrow, const int32_t* __restrict__ off,
                                      const int32_t* __restrict__ col,
@@ -1681,6 +1798,16 @@ extern "C" int gbpc_convert_factor(int n, const int32_t* offsets, const int32_t*
 // Fixed-support refit entry points (fsai_reuse.py:157-245).
 
 namespace gbpc {
+// GBPC_FSAI_REFIT_WIDE=0 keeps supports wider than 16 on the warp-per-row
+// refit (the two give identical values; the switch exists to compare them).
+static bool refit_wide_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBPC_FSAI_REFIT_WIDE");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <typename T, typename S>
 static int refit_t(int n, const int32_t* a_off, const int32_t* a_col, const T* a_val,
                    const int32_t* g_off, const int32_t* g_col, int width, double floor_, S* out,
@@ -1700,6 +1827,36 @@ static int refit_t(int n, const int32_t* a_off, const int32_t* a_col, const T* a
     } else if (width <= 16) {
       fsai_refit_row_kernel<T, S, 16><<<grid_for(n, 128), 128, 0, st>>>(
           n, a_off, a_col, a_val, scale.as<T>(), g_off, g_col, (T)floor_, out, stat + 1);
+    } else if (refit_wide_enabled()) {
+      // Thread per row, rows in order of support size, the local factors of
+      // a chunk of rows in device memory (a quarter of the free memory, 8 GB
+      // at most).
+      const int ft = 128;
+      const size_t tri = (size_t)width * (width + 1) / 2;
+      size_t free_b = 0, total_b = 0;
+      GBPC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+      const size_t budget = std::min<size_t>(free_b / 4, (size_t)8 << 30);
+      const int nc = (int)std::min<int64_t>(
+          n, std::max<int64_t>(4096, (int64_t)(budget / (sizeof(T) * tri))));
+      DevBuf bins, order, lbuf;
+      if ((rc = bins.alloc(sizeof(int32_t) * (width + 1))) ||
+          (rc = order.alloc(sizeof(int32_t) * n)) || (rc = lbuf.alloc(sizeof(T) * tri * nc)))
+        return rc;
+      GBPC_CUDA_TRY(cudaMemsetAsync(bins.p, 0, sizeof(int32_t) * (width + 1), st));
+      support_size_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, g_off, width,
+                                                                  bins.as<int32_t>());
+      support_size_scan_kernel<<<1, 32, 0, st>>>(width, bins.as<int32_t>());
+      support_size_scatter_kernel<<<grid_for(n, 256), 256, 0, st>>>(
+          n, g_off, width, bins.as<int32_t>(), order.as<int32_t>());
+      const size_t smem = sizeof(T) * (size_t)width * ft;
+      GBPC_CUDA_TRY(cudaFuncSetAttribute(fsai_refit_wide_kernel<T, S>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      for (int k0 = 0; k0 < n; k0 += nc) {
+        const int cnt = std::min(nc, n - k0);
+        fsai_refit_wide_kernel<T, S><<<grid_for(cnt, ft), ft, smem, st>>>(
+            cnt, order.as<int32_t>() + k0, (int64_t)cnt, lbuf.as<T>(), a_off, a_col, a_val,
+            scale.as<T>(), g_off, g_col, width, (T)floor_, out, stat + 1);
+      }
     } else {
       const size_t smem = sizeof(T) * (size_t)(width * (width + 1) / 2 + width) * kRefitWarps;
       GBPC_CUDA_TRY(cudaFuncSetAttribute(fsai_refit_kernel<T, S>,

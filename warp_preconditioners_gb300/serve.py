@@ -9,9 +9,10 @@ that cannot fit at all is rejected) and runs requests in slots, one CUDA
 stream each.  A free slot takes the oldest queued request whose system is
 idle, copies its right-hand sides in, runs the whole PCG loop as one CUDA
 graph (k > 1: the batched solver, which reads the matrices once per
-iteration for all k right-hand sides; k = 1: the single-vector solver; a
-small system's solves run on thread-block clusters instead, one kernel for
-the whole solve, one cluster per right-hand side in one launch),
+iteration for all k right-hand sides; k = 1: the single-vector solver, which
+runs a small system's whole solve as one kernel on a thread-block cluster;
+with ``GpuExecutor(cluster_rhs=True)`` a small system's k > 1 right-hand
+sides also run that way, one cluster each in one launch),
 copies x back, and is free for the next request as soon as its event fires.
 Requests join and leave the running set one by one, so none waits for a
 batch to fill or for an unrelated long solve.
@@ -214,7 +215,7 @@ class ResidentSystem:
     """Device-resident operator, FSAI factor and Krylov state of one system."""
 
     def __init__(self, host: HostSystem, *, width: int = 8, step: int = 1, kap: float = 1e-3,
-                 max_rhs: int = MAX_RHS, batched: bool = True, cluster_rhs: bool = True,
+                 max_rhs: int = MAX_RHS, batched: bool = True, cluster_rhs: bool = False,
                  device="cuda"):
         from .batched import BatchedCG, batched_fsai, batched_sparse, batched_sqlap
         from .fsai import FSAI
@@ -379,7 +380,7 @@ class GpuExecutor:
     def __init__(self, catalog: Catalog, *, slots: int = 16, sequential: bool = False,
                  tol: float = 1e-8, maxiter: int = 0, width: int = 8, step: int = 1,
                  kap: float = 1e-3, max_rhs: int = MAX_RHS, merge_rhs: int = 0,
-                 cluster_rhs: bool = True, device="cuda"):
+                 cluster_rhs: bool = False, device="cuda"):
         if not torch.cuda.is_available():
             raise RuntimeError("GpuExecutor needs a CUDA device")
         if merge_rhs and not 2 <= merge_rhs <= 32:
@@ -393,8 +394,8 @@ class GpuExecutor:
         # to merge_rhs right-hand sides (0: one request per solve).
         self.merge_rhs = 0 if sequential else int(merge_rhs)
         self.max_rhs = max(max_rhs, self.merge_rhs)
-        # Small systems run a request's k right-hand sides as k cluster solves
-        # in one launch (False: the batched solver, as for large systems).
+        # cluster_rhs: a small system runs a request's k right-hand sides as k
+        # cluster solves in one launch, instead of the batched solver.
         self.cluster_rhs = bool(cluster_rhs)
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(self.slots)]
