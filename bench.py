@@ -86,6 +86,8 @@ def parse_args():
     p.add_argument("--c5-nmax", type=float, default=5e5)
     p.add_argument("--c5-no-sequential", action="store_true",
                    help="skip the one-at-a-time float64 arm")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the C1 and C3 sub-measurements of the default line")
     p.add_argument("--no-mixed", action="store_true",
                    help="skip the mixed-precision 32-RHS batched measurement")
     p.add_argument("--fp32-refinement", action="store_true",
@@ -483,6 +485,11 @@ def main():
         line["wide_fsai"] = measure_wide_fsai(args, prob, Q, K, mass, free, dev, ms_per_step)
         line["multi_system"] = measure_multi_system(dev)
         line["multi_system_small"] = measure_multi_system(dev, sides=(17, 18, 19, 20) * 8)
+    if not args.no_configs:
+        # The reference's CPU-runnable case and its block-coupling benchmark,
+        # measured in the same run (their own configs: --config c1 / c3).
+        line["c1"] = run_c1(args, dev)
+        line["c3"] = run_c3(args, dev)
     line["refit"] = measure_refit(args, prob, Q, dev)
     line["assembly"] = measure_assembly(prob, dev)
     if args.lifted:
