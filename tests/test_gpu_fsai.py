@@ -156,17 +156,27 @@ def test_biharmonic_tet_cube_bit_exact(oracle, width, step):
 
 @pytest.mark.parametrize("width,step", [(8, 2), (16, 2)])
 def test_wide_frontier_overflow_rerun_bit_exact(oracle, width, step):
-    # ~160 entries per row: frontiers exceed the first pass's candidate
-    # table, so those rows are rebuilt by the rerun with a larger table.
+    # ~290 entries per row: frontiers exceed the first pass's candidate
+    # table (512 slots), so those rows are rebuilt by the rerun with a table
+    # that cannot overflow.
     from warp_preconditioners_gb300 import FSAI
 
     rng = np.random.default_rng(83)
-    n = 400
-    m = ss.random(n, n, density=0.2, random_state=rng, data_rvs=lambda k: rng.uniform(-1, 1, k))
+    n = 1500
+    m = ss.random(n, n, density=0.1, random_state=rng, data_rvs=lambda k: rng.uniform(-1, 1, k))
     a = (m + m.T).tocsr()
     a = a + ss.diags(np.abs(a).sum(axis=1).A1 + 1.0)
+    a.sort_indices()
     pre = FSAI(to_bsr(a), max_row_size=width, max_step_size=step, kap_tolerance=0.0)
     g_or, gt_or, trunc = oracle.fsai(oracle_csr(oracle, a), width=width, step=step, tol=0.0)
+    # Some row's final support meets more distinct columns below it than the
+    # first table holds, so the rerun ran.
+    widest = 0
+    for i in range(0, n, 7):
+        sup = g_or.columns[g_or.offsets[i]:g_or.offsets[i + 1]]
+        cols = np.unique(np.concatenate([a.indices[a.indptr[c]:a.indptr[c + 1]] for c in sup]))
+        widest = max(widest, int((cols < i).sum()) + len(sup))
+    assert widest > 512
     assert pre.truncated_rows == trunc
     assert_same_factor(pre.G, g_or)
     assert_same_factor(pre.GT, gt_or)

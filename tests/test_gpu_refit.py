@@ -197,3 +197,28 @@ def test_empty_reusable_fsai():
         v = torch.empty(0, dtype=dtype, device=dev)
         pre.matvec(v, v, v, 1.0, 0.0)
         torch.cuda.synchronize()
+
+
+def test_build_and_refit_in_chunks(oracle, monkeypatch):
+    # The build by rounds and the wide refit hold the device state of a
+    # chunk of rows at a time (GBPC_FSAI_CHUNK_ROWS caps it); four chunks of
+    # the 12^3 cube give the oracle's factor and refit bit for bit.
+    from warp_preconditioners_gb300 import FSAI, problems
+
+    _, _, K, mass = problems.tet_cube(12)
+    q1 = problems.biharmonic(K, mass, 1e-4)
+    q2 = problems.biharmonic(K, mass, 3e-3)
+    monkeypatch.setenv("GBPC_FSAI_CHUNK_ROWS", "500")
+    pre = FSAI(to_bsr(q1), max_row_size=24, max_step_size=2, kap_tolerance=1e-3,
+               reuse_pattern=True)
+    g_or, _, trunc = oracle.fsai(oracle_csr(oracle, q1), width=24, step=2, tol=1e-3)
+    off, col, val = host_csr(pre.G)
+    np.testing.assert_array_equal(off, g_or.offsets)
+    np.testing.assert_array_equal(col, g_or.columns)
+    np.testing.assert_array_equal(val, g_or.values)
+    assert pre.truncated_rows == trunc
+    pre.update(to_bsr(q2))
+    off, col, val = host_csr(pre.G)
+    expected, bd, br = oracle.fsai_refit(oracle_csr(oracle, q2), oracle.CSR(off, col, val))
+    assert bd == br == 0
+    np.testing.assert_array_equal(val, expected)

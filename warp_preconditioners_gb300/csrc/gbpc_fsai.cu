@@ -29,6 +29,7 @@
 // SPD input assembled by summation is); other inputs are rejected.
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <vector>
 
@@ -1387,6 +1388,15 @@ __global__ void scatter_values_kernel(int64_t count, const V* __restrict__ src,
 // ---------------------------------------------------------------------------
 // Host entry points.
 
+// GBPC_FSAI_CHUNK_ROWS=m caps the rows whose device state the build by
+// rounds and the wide refit hold at once (read on every call; the tests use
+// it to run several chunks on small matrices).
+static int64_t chunk_rows_limit() {
+  const char* e = std::getenv("GBPC_FSAI_CHUNK_ROWS");
+  const long long v = e ? std::atoll(e) : 0;
+  return v >= 32 ? (int64_t)v : INT64_MAX;
+}
+
 // GBPC_FSAI_ROUNDS=0 selects the warp-per-row build for every row (the two
 // builds give identical factors; the switch exists to compare them).
 static bool rounds_build_enabled() {
@@ -1499,7 +1509,7 @@ static int fsai_setup_t(int n, const int32_t* off, const int32_t* col, const T* 
     GBPC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     const size_t budget = std::min<size_t>(free_b / 4, (size_t)8 << 30);
     const int64_t cap = std::max<int64_t>(4096, (int64_t)(budget / per_row));
-    const int nc = (int)std::min<int64_t>(n, cap);
+    const int nc = (int)std::min<int64_t>(n, std::min<int64_t>(cap, chunk_rows_limit()));
     DevBuf b_size, b_nsel, b_flags, b_pat, b_lo, b_cand, b_z, b_v, b_L, b_a, b_l0, b_l1, b_count;
     if ((rc = b_size.alloc(sizeof(int32_t) * nc)) || (rc = b_nsel.alloc(sizeof(int32_t) * nc)) ||
         (rc = b_flags.alloc(sizeof(int32_t) * nc)) ||
@@ -1837,7 +1847,8 @@ static int refit_t(int n, const int32_t* a_off, const int32_t* a_col, const T* a
       GBPC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
       const size_t budget = std::min<size_t>(free_b / 4, (size_t)8 << 30);
       const int nc = (int)std::min<int64_t>(
-          n, std::max<int64_t>(4096, (int64_t)(budget / (sizeof(T) * tri))));
+          n, std::min<int64_t>(std::max<int64_t>(4096, (int64_t)(budget / (sizeof(T) * tri))),
+                               chunk_rows_limit()));
       DevBuf bins, order, lbuf;
       if ((rc = bins.alloc(sizeof(int32_t) * (width + 1))) ||
           (rc = order.alloc(sizeof(int32_t) * n)) || (rc = lbuf.alloc(sizeof(T) * tri * nc)))
