@@ -138,8 +138,8 @@ def test_zero_tolerance_full_width(golden):
     np.testing.assert_allclose(g.T @ g, d["inv32"], rtol=1e-12, atol=1e-15)
 
 
-@pytest.mark.parametrize("width,step", [(8, 1), (8, 2), (12, 2), (16, 1), (16, 3), (48, 1),
-                                        (48, 2), (64, 3)])
+@pytest.mark.parametrize("width,step", [(1, 1), (2, 1), (3, 5), (8, 1), (8, 2), (12, 2),
+                                        (16, 1), (16, 3), (48, 1), (48, 2), (64, 3), (64, 64)])
 def test_biharmonic_tet_cube_bit_exact(oracle, width, step):
     # The assembled smoothing operator of the benchmark, on a small cube:
     # 65-entry rows, exact ties, numerically nonsymmetric SpGEMM values.
