@@ -81,6 +81,11 @@ def parse_args():
     p.add_argument("--c5-cluster-small", action="store_true",
                    help="also serve with small systems' multi-RHS requests as one cluster "
                         "solve per right-hand side instead of the batched solver")
+    p.add_argument("--c5-wide-from", type=int, default=0,
+                   help="also serve with FSAI width 48 for systems of at least this many "
+                        "unknowns (0: skip that arm)")
+    p.add_argument("--c5-wide-step", type=int, default=2,
+                   help="max_step_size of the width-48 factors of that arm")
     p.add_argument("--c5-budget-gb", type=float, default=120.0)
     p.add_argument("--c5-nmin", type=float, default=5e3)
     p.add_argument("--c5-nmax", type=float, default=5e5)
@@ -1331,30 +1336,38 @@ def run_c5(args, dev):
     # max_i |b - A x|_i / (|A| |x| + |b|)_i.  For the alpha = 1e-4 biharmonic
     # systems the first is dominated by cancellation in forming b - A x
     # (|A| |x| >> |b|); the second is the accuracy measure.
-    acc = {kind: {"rel": [], "berr": []} for kind in serve.KINDS}
-    nonfinite = 0
     assembled = {}
-    for req, r in zip(stream, served):
-        if r.ok and r.x is not None:
-            h = cat.get(req.key)
-            if req.key not in assembled:  # host assembly for the check only
-                assembled[req.key] = h.assembled()
-            A = assembled[req.key]
-            b, x = serve.request_rhs(req).numpy(), r.x.numpy()
-            if not np.isfinite(x).all():
-                nonfinite += 1
-                continue
-            res = b - A @ x
-            acc[h.kind]["rel"].append(float((np.linalg.norm(res, axis=0)
-                                             / np.linalg.norm(b, axis=0)).max()))
-            den = abs(A) @ np.abs(x) + np.abs(b)
-            acc[h.kind]["berr"].append(float((np.abs(res) / den).max()))
-    out["served"]["checked_requests"] = sum(len(a["rel"]) for a in acc.values()) + nonfinite
-    out["served"]["nonfinite_solutions"] = nonfinite
-    out["served"]["accuracy_sampled"] = {
-        kind: {"requests": len(a["rel"]), "relres_max": max(a["rel"]) if a["rel"] else None,
-               "backward_error_max": max(a["berr"]) if a["berr"] else None}
-        for kind, a in acc.items()}
+
+    def sample_accuracy(reqs, results):
+        acc = {kind: {"rel": [], "berr": []} for kind in serve.KINDS}
+        nonfinite = 0
+        for req, r in zip(reqs, results):
+            if r.ok and r.x is not None:
+                h = cat.get(req.key)
+                if req.key not in assembled:  # host assembly for the check only
+                    assembled[req.key] = h.assembled()
+                A = assembled[req.key]
+                b, x = serve.request_rhs(req).numpy(), r.x.numpy()
+                if not np.isfinite(x).all():
+                    nonfinite += 1
+                    continue
+                res = b - A @ x
+                acc[h.kind]["rel"].append(float((np.linalg.norm(res, axis=0)
+                                                 / np.linalg.norm(b, axis=0)).max()))
+                den = abs(A) @ np.abs(x) + np.abs(b)
+                acc[h.kind]["berr"].append(float((np.abs(res) / den).max()))
+        summary = {kind: {"requests": len(a["rel"]),
+                          "relres_max": max(a["rel"]) if a["rel"] else None,
+                          "backward_error_max": max(a["berr"]) if a["berr"] else None}
+                   for kind, a in acc.items()}
+        summary["checked_requests"] = sum(len(a["rel"]) for a in acc.values()) + nonfinite
+        summary["nonfinite_solutions"] = nonfinite
+        return summary
+
+    sampled = sample_accuracy(stream, served)
+    out["served"]["checked_requests"] = sampled.pop("checked_requests")
+    out["served"]["nonfinite_solutions"] = sampled.pop("nonfinite_solutions")
+    out["served"]["accuracy_sampled"] = sampled
 
     if args.c5_merge:
         mex = serve.GpuExecutor(cat, slots=args.c5_slots, tol=args.rtol, device=dev,
@@ -1376,6 +1389,19 @@ def run_c5(args, dev):
         out["served_cluster_small"] = serve.summarize(bsrv.run(stream, keep=lambda r: False))
         out["served_cluster_small_burst"] = serve.summarize(bsrv.run(burst, keep=lambda r: False))
         del bsrv, bex
+    if args.c5_wide_from:
+        wex = serve.GpuExecutor(cat, slots=args.c5_slots, tol=args.rtol, device=dev,
+                                wide_from=args.c5_wide_from, wide_step=args.c5_wide_step)
+        wsrv = serve.Server(wex, budget_bytes=budget)
+        t0 = time.perf_counter()
+        wsrv.prepare(keys)
+        torch.cuda.synchronize()
+        out["served_wide_setup_s"] = time.perf_counter() - t0
+        wide_res = wsrv.run(stream, keep=keep)
+        out["served_wide"] = serve.summarize(wide_res)
+        out["served_wide"]["accuracy_sampled"] = sample_accuracy(stream, wide_res)
+        out["served_wide_burst"] = serve.summarize(wsrv.run(burst, keep=lambda r: False))
+        del wsrv, wex
     if not args.c5_no_sequential:
         seq_ex = serve.GpuExecutor(cat, sequential=True, tol=args.rtol, device=dev)
         seq = serve.Server(seq_ex, budget_bytes=budget)
@@ -1386,6 +1412,11 @@ def run_c5(args, dev):
         sb, qb = out["served_burst"], out["sequential_burst"]
         out["speedup"] = {"capacity_solves_per_s": sb["solves_per_s"] / qb["solves_per_s"],
                           "p50": q["p50_ms"] / s["p50_ms"], "p99": q["p99_ms"] / s["p99_ms"]}
+        if args.c5_wide_from:
+            mb, m = out["served_wide_burst"], out["served_wide"]
+            out["speedup_wide"] = {
+                "capacity_solves_per_s": mb["solves_per_s"] / qb["solves_per_s"],
+                "p50": q["p50_ms"] / m["p50_ms"], "p99": q["p99_ms"] / m["p99_ms"]}
         if args.c5_cluster_small:
             mb, m = out["served_cluster_small_burst"], out["served_cluster_small"]
             out["speedup_cluster_small"] = {

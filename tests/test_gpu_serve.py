@@ -128,3 +128,18 @@ def test_merged_requests_match_alone_within_tolerance(catalog):
         b = serve.request_rhs(req).numpy()
         res = np.linalg.norm(b - A @ x, axis=0) / np.linalg.norm(b, axis=0)
         assert res.max() < 50 * TOL, (req, res)
+
+
+def test_wide_factors_for_large_systems_meet_tolerance(catalog):
+    # Systems at or above wide_from get a width-48 factor (grown two entries
+    # a step); every request still meets the solve tolerance.
+    stream = small_stream()
+    ex = serve.GpuExecutor(catalog, slots=4, tol=TOL, wide_from=1)
+    assert all(ex.width_for(catalog.get(r.key)) == 48 for r in stream)
+    served = serve.Server(ex).run(stream)
+    for req, r in zip(stream, served):
+        assert r.ok, r.error
+        A = host_matrix(catalog.get(req.key))
+        b = serve.request_rhs(req).numpy()
+        res = np.linalg.norm(b - A @ r.x.numpy(), axis=0) / np.linalg.norm(b, axis=0)
+        assert res.max() < 50 * TOL, (req, res)

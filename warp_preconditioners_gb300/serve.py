@@ -380,7 +380,8 @@ class GpuExecutor:
     def __init__(self, catalog: Catalog, *, slots: int = 16, sequential: bool = False,
                  tol: float = 1e-8, maxiter: int = 0, width: int = 8, step: int = 1,
                  kap: float = 1e-3, max_rhs: int = MAX_RHS, merge_rhs: int = 0,
-                 cluster_rhs: bool = False, device="cuda"):
+                 cluster_rhs: bool = False, wide_from: int = 0, wide_width: int = 48,
+                 wide_step: int = 2, device="cuda"):
         if not torch.cuda.is_available():
             raise RuntimeError("GpuExecutor needs a CUDA device")
         if merge_rhs and not 2 <= merge_rhs <= 32:
@@ -397,11 +398,24 @@ class GpuExecutor:
         # cluster_rhs: a small system runs a request's k right-hand sides as k
         # cluster solves in one launch, instead of the batched solver.
         self.cluster_rhs = bool(cluster_rhs)
+        # wide_from > 0: systems of at least that many unknowns get an FSAI
+        # factor of width wide_width grown wide_step entries at a time (fewer
+        # iterations for a longer setup, paid once while the system is
+        # resident).
+        self.wide_from, self.wide_width, self.wide_step = (int(wide_from), int(wide_width),
+                                                           int(wide_step))
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(self.slots)]
 
+    def _wide(self, host: HostSystem) -> bool:
+        return self.wide_from > 0 and host.n >= self.wide_from
+
+    def width_for(self, host: HostSystem) -> int:
+        return self.wide_width if self._wide(host) else self.width
+
     def estimate(self, key) -> int:
-        return estimate_bytes(self.catalog.get(key), self.max_rhs, self.width)
+        host = self.catalog.get(key)
+        return estimate_bytes(host, self.max_rhs, self.width_for(host))
 
     def build(self, key):
         from . import _lib
@@ -410,7 +424,8 @@ class GpuExecutor:
         cur = torch.cuda.current_stream(self.device)
         cur.synchronize()
         m0, l0 = torch.cuda.memory_allocated(self.device), _lib.live_device_bytes()
-        res = ResidentSystem(host, width=self.width, step=self.step, kap=self.kap,
+        res = ResidentSystem(host, width=self.width_for(host),
+                             step=self.wide_step if self._wide(host) else self.step, kap=self.kap,
                              max_rhs=self.max_rhs, batched=not self.sequential,
                              cluster_rhs=self.cluster_rhs, device=self.device)
         res.warm(self.tol)
