@@ -444,7 +444,10 @@ def main():
 
     apply = measure_applies(
         pre, lambda: FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
-                          kap_tolerance=1e-3), K, mass, free, n, dev)
+                          kap_tolerance=1e-3), K, mass, free, n, dev,
+        make_low=lambda: FSAI(Q, max_row_size=args.width, max_step_size=args.step_size,
+                              kap_tolerance=1e-3, factor_dtype=torch.bfloat16,
+                              apply_dtype=torch.float32))
     traffic = read_traffic()
     fp64_peak = measure_fp64_peak(dev)
 
@@ -1477,7 +1480,7 @@ def _graph_time(fns, reps, dev):
     return s.elapsed_time(e) / reps / 1e3
 
 
-def measure_applies(pre, make_pre, K, mass, free, n, dev, copies=5):
+def measure_applies(pre, make_pre, K, mass, free, n, dev, copies=5, make_low=None):
     """Live CUDA-event timing of the two applies on the step's data,
     algorithmic bytes over the time (GB/s), two ways:
 
@@ -1488,6 +1491,10 @@ def measure_applies(pre, make_pre, K, mass, free, n, dev, copies=5):
       vectors (more than twice the 129 MB L2 in total), so every apply reads
       its matrices from HBM.  Reuse inside one apply (the factored operator
       reads its one copy of L twice) still counts, as it does in a solve.
+
+    ``fsai_apply_bf16_f32``: the same FSAI factor stored in bfloat16 and
+    applied in float32 behind the float64 interface (x read as float64, the
+    intermediate G x as float32, z written as float64); no FP64 arithmetic.
     """
     import torch
 
@@ -1517,6 +1524,18 @@ def measure_applies(pre, make_pre, K, mass, free, n, dev, copies=5):
         out[name] = {"us": t_res * 1e6, "gbps": nbytes / t_res / 1e9, "bytes": nbytes,
                      "hbm": {"us": t_hbm * 1e6, "gbps": nbytes / t_hbm / 1e9,
                              "copies": copies, "rotated_bytes": copies * footprint}}
+    if make_low is not None:
+        lows = [make_low() for _ in range(copies)]
+        low = lows[0]
+        nbytes = (low.G.nnz + low.GT.nnz) * 6 + 2 * 4 * (n + 1) + n * (8 + 4 + 4 + 8)
+        calls = [(lambda c: lambda: lows[c].matvec(xs[c], xs[c], zs[c], 1.0, 0.0))(c)
+                 for c in range(copies)]
+        t_res = _graph_time(calls[:1], reps, dev)
+        t_hbm = _graph_time(calls, reps, dev)
+        out["fsai_apply_bf16_f32"] = {
+            "us": t_res * 1e6, "gbps": nbytes / t_res / 1e9, "bytes": nbytes,
+            "hbm": {"us": t_hbm * 1e6, "gbps": nbytes / t_hbm / 1e9, "copies": copies,
+                    "rotated_bytes": copies * nbytes}}
     return out
 
 
