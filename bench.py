@@ -777,12 +777,21 @@ def _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step, pre_kw, solver
 def measure_wide_fsai(args, prob, Q, K, mass, free, dev, ms_per_step):
     """The default step with the wide factors the reference's sweep uses
     (width 48, steps 1 and 2): fewer CG iterations for a longer setup."""
+    import torch
+
     out = {}
     for step in (1, 2):
         out[f"w48_step{step}"] = _step_variant(args, prob, Q, K, mass, free, dev, ms_per_step,
                                                dict(max_row_size=48, max_step_size=step), {})
+    for name, dt in (("bf16", torch.bfloat16), ("f32", torch.float32)):
+        out[f"w48_step2_{name}_f32apply"] = _step_variant(
+            args, prob, Q, K, mass, free, dev, ms_per_step,
+            dict(max_row_size=48, max_step_size=2, factor_dtype=dt, apply_dtype=torch.float32),
+            {})
     out["solver"] = ("the default step (FSAI setup + 4 sequential CG solves) with "
-                     "FSAI(Q, max_row_size=48, max_step_size=1 or 2, kap_tolerance=1e-3)")
+                     "FSAI(Q, max_row_size=48, max_step_size=1 or 2, kap_tolerance=1e-3); "
+                     "*_f32apply: the step-2 factor stored in bf16 / f32 and applied in float32 "
+                     "(operator, recurrences and dots float64)")
     return out
 
 
