@@ -627,16 +627,16 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             its.append(nit)
         return xs, its
 
-    def batch64():
-        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3)
+    def batch64(width=args.width, step=args.step_size):
+        pre = FSAI(Q, max_row_size=width, max_step_size=step, kap_tolerance=1e-3)
         bs = batched.BatchedSolver(K, mass, ALPHA, pre)
         X = torch.zeros_like(B)
         nit, _ = bs.solve(B, X, tol=args.rtol, maxiter=100000)
         return X, nit.clone()
 
-    def batch_f32m(factor_dtype):
+    def batch_f32m(factor_dtype, width=args.width, step=args.step_size):
         # The batched operator narrows the float32 factor to factor_dtype itself.
-        pre = FSAI(Q, max_row_size=args.width, max_step_size=args.step_size, kap_tolerance=1e-3,
+        pre = FSAI(Q, max_row_size=width, max_step_size=step, kap_tolerance=1e-3,
                    factor_dtype=torch.float32)
         bs = batched.BatchedSolver(K, mass, ALPHA, pre, factor_dtype=factor_dtype,
                                    apply_dtype=torch.float32)
@@ -666,6 +666,11 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
     t_plain, (xs, its) = timed(plain)
     t_batch, (Xb, nitb) = timed(batch64)
     low = {dt: timed(lambda: batch_f32m(dt)) for dt in (torch.bfloat16, torch.float32)}
+    # The same batched solves with the width-48, step-2 factor.
+    batch64(48, 2)
+    batch_f32m(torch.bfloat16, 48, 2)
+    wide = {"fp64": timed(lambda: batch64(48, 2)),
+            "bf16_f32apply": timed(lambda: batch_f32m(torch.bfloat16, 48, 2))}
     if args.fp32_refinement:
         t_mixed, (Xm, outer, inner) = timed(mixed)
     qh = prob["Q"]
@@ -704,6 +709,16 @@ def run_mixed_batched(args, prob, Q, K, mass, free, dev, k=32):
             "speedup_vs_batched_fp64": t_batch / t_low,
             "iterations_max": int(nitl.max().item()), "backward_error_max": berr_l,
             "rel_diff_vs_plain_max": rel_l}
+    for name, (t_w, (Xw, nitw)) in wide.items():
+        berr_w, rel_w = quality(Xw.cpu().numpy())
+        out[f"batched_w48_step2_{name}"] = {
+            "solver": (f"one batched float64 PCG for all {k} RHS with FSAI width 48, step 2"
+                       + (", the factor stored in bf16 and applied in float32"
+                          if name != "fp64" else "")),
+            "ms": t_w, "solves_per_s": k / (t_w / 1e3), "speedup": t_plain / t_w,
+            "speedup_vs_batched_fp64": t_batch / t_w,
+            "iterations_max": int(nitw.max().item()), "backward_error_max": berr_w,
+            "rel_diff_vs_plain_max": rel_w}
     if args.fp32_refinement:
         berr_m, rel_m = quality(Xm.cpu().numpy())
         out["float32_refinement"] = {
