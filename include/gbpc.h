@@ -86,7 +86,12 @@ int gbpc_device_bytes(size_t* live_host);
  * status_host[3] receives the reference's counters: [0] invalid diagonals,
  * [1] truncated rows (pivot guard), [2] rows that lost finiteness or a
  * positive diagonal.  Returns GBPC_ERR_DIAGONAL / GBPC_ERR_FACTOR when the
- * reference raises.  Synchronises `stream`. */
+ * reference raises.  Synchronises `stream`.  Temporary device memory, freed
+ * before returning: the equilibrated entries (2 nnz values) and, for the rows
+ * being built at once, each row's local factor, vectors and gathered entries
+ * ((width (width + 1) / 2 + (2 + min(step, width)) width) values and
+ * 2 width + 8 ints per row; at most a quarter of the free memory and 8 GB,
+ * rows taken in chunks beyond that). */
 int gbpc_fsai_setup(int n, const int32_t* offsets, const int32_t* columns, const void* values,
                     int dtype, int width, int step, double kap_tolerance, double pivot_floor,
                     int32_t* ell_cols, void* ell_vals, int32_t* row_counts, void* scale,
