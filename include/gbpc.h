@@ -90,8 +90,8 @@ int gbpc_device_bytes(size_t* live_host);
  * before returning: the equilibrated entries (2 nnz values) and, for the rows
  * being built at once, each row's local factor, vectors and gathered entries
  * ((width (width + 1) / 2 + (2 + min(step, width)) width) values and
- * 2 width + 8 ints per row; at most a quarter of the free memory and 8 GB,
- * rows taken in chunks beyond that). */
+ * 2 width + min(step, width) + 5 ints per row; at most a quarter of the free
+ * memory and 8 GB, rows taken in chunks beyond that). */
 int gbpc_fsai_setup(int n, const int32_t* offsets, const int32_t* columns, const void* values,
                     int dtype, int width, int step, double kap_tolerance, double pivot_floor,
                     int32_t* ell_cols, void* ell_vals, int32_t* row_counts, void* scale,
