@@ -137,7 +137,10 @@ int gbpc_convert_factor(int n, const int32_t* offsets, const int32_t* columns, c
  * float32 / bfloat16).  G itself is not touched.  status_host[0] counts
  * non-finite or non-positive diagonals of A, status_host[1] rows with a
  * pivot <= pivot_floor, a non-finite value or a non-positive diagonal; the
- * caller publishes `out` only when both are zero.  Synchronises. */
+ * caller publishes `out` only when both are zero.  Synchronises.  For width
+ * > 16 it allocates temporary device memory for the local factors of the
+ * rows refitted at once (width (width + 1) / 2 values per row; at most a
+ * quarter of the free memory and 8 GB, rows taken in chunks beyond that). */
 int gbpc_fsai_refit(int n, const int32_t* a_off, const int32_t* a_col, const void* a_val,
                     int dtype, const int32_t* g_off, const int32_t* g_col, int width,
                     double pivot_floor, void* out, int factor_dtype, int32_t* status_host,
