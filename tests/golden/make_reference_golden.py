@@ -12,9 +12,9 @@ preconditioners on seeded inputs and stores inputs and outputs in
   warp_preconditioners/fsai.py: build kernel, pack_factor, bsr_transposed)
   of the 64 x 64 five-point Laplacian (width 8, step 1), of the assembled
   biharmonic ``Q = alpha M + K M^-1 K`` on an 8^3 jittered tet cube (widths
-  8/16/48, steps 1/2, a float32 factor at kap 3e-3), and the fixed-support
-  refit of that factor for Q at 2 alpha (``FSAI.update``,
-  warp_preconditioners/fsai_reuse.py).
+  8/16/48/64, steps 1/2, a float32 factor at kap 3e-3), and the
+  fixed-support refit of the width-8 and the width-48 factor for Q at
+  2 alpha (``FSAI.update``, warp_preconditioners/fsai_reuse.py).
 * ``ref_block.npz``: on A = K (x) C (K the 7-point Laplacian on 6^3 nodes,
   C = R diag(1, 1, 1e-6) R^T): BlockJacobi inverses
   (warp_preconditioners/block_ilu.py), BlockILU0 factors with 3 factor sweeps
@@ -94,7 +94,7 @@ def fsai_cases():
     Q = problems.biharmonic(K, mass, ALPHA)
     put_csr(out, "cube8_Q", Q.indptr, Q.indices, Q.data)
     for width, step, kap, fdt in [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 2, 1e-3, None),
-                                  (8, 1, 3e-3, wp.float32)]:
+                                  (64, 1, 1e-3, None), (8, 1, 3e-3, wp.float32)]:
         t = time.time()
         pre = FSAI(from_scipy(Q), max_row_size=width, kap_tolerance=kap, max_step_size=step,
                    factor_dtype=fdt)
@@ -111,6 +111,14 @@ def fsai_cases():
     pre.update(from_scipy(Q2))
     put_bsr(out, "cube8_refit_G", pre.G)
     put_bsr(out, "cube8_refit_GT", pre.GT)
+    # The same refit on the wide (width 48, step 2) supports.
+    t = time.time()
+    pre = FSAI(from_scipy(Q), max_row_size=48, kap_tolerance=1e-3, max_step_size=2,
+               reuse_pattern=True)
+    pre.update(from_scipy(Q2))
+    put_bsr(out, "cube8_refit48_G", pre.G)
+    put_bsr(out, "cube8_refit48_GT", pre.GT)
+    print(f"cube8 refit w48 s2: nnz {pre.G.nnz} ({time.time() - t:.1f} s)", flush=True)
     np.savez_compressed(HERE / "ref_fsai.npz", **out)
 
 

@@ -22,7 +22,7 @@ from gpu_helpers import cuda, host_csr, vec
 pytestmark = pytest.mark.gpu
 
 REF_FSAI = [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 2, 1e-3, None),
-            (8, 1, 3e-3, torch.float32)]
+            (64, 1, 1e-3, None), (8, 1, 3e-3, torch.float32)]
 
 
 def _bits(a):
@@ -88,14 +88,16 @@ def test_fsai_tet_cube_biharmonic(ref_fsai, width, step, kap, fdt):
     assert pre.truncated_rows == int(ref_fsai[tag + "_truncated"])
 
 
-def test_fsai_refit(ref_fsai):
+@pytest.mark.parametrize("width,step,tag", [(8, 1, "cube8_refit"), (48, 2, "cube8_refit48")])
+def test_fsai_refit(ref_fsai, width, step, tag):
+    # Width 48 runs the wide refit (a thread per row, factors in device memory).
     from warp_preconditioners_gb300 import FSAI
 
-    pre = FSAI(_matrix(ref_fsai, "cube8_Q"), max_row_size=8, kap_tolerance=1e-3,
-               reuse_pattern=True)
+    pre = FSAI(_matrix(ref_fsai, "cube8_Q"), max_row_size=width, kap_tolerance=1e-3,
+               max_step_size=step, reuse_pattern=True)
     pre.update(_matrix(ref_fsai, "cube8_Q2"))
-    assert_factor_equal(pre.G, ref_fsai, "cube8_refit_G")
-    assert_factor_equal(pre.GT, ref_fsai, "cube8_refit_GT")
+    assert_factor_equal(pre.G, ref_fsai, tag + "_G")
+    assert_factor_equal(pre.GT, ref_fsai, tag + "_GT")
 
 
 def test_block_jacobi_and_ilu0(ref_block):

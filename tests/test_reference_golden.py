@@ -20,7 +20,7 @@ import pytest
 from conftest import GOLDEN
 
 REF_FSAI = [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 2, 1e-3, None),
-            (8, 1, 3e-3, np.float32)]
+            (64, 1, 1e-3, None), (8, 1, 3e-3, np.float32)]
 
 
 def _csr(o, f, p):
@@ -89,12 +89,13 @@ def test_fsai_tet_cube_biharmonic(oracle, ref_fsai, width, step, kap, fdt):
     assert trunc == int(ref_fsai[tag + "_truncated"])
 
 
-def test_fsai_refit(oracle, ref_fsai):
-    g, _, _ = oracle.fsai(_csr(oracle, ref_fsai, "cube8_Q"), width=8)
+@pytest.mark.parametrize("width,step,tag", [(8, 1, "cube8_refit"), (48, 2, "cube8_refit48")])
+def test_fsai_refit(oracle, ref_fsai, width, step, tag):
+    g, _, _ = oracle.fsai(_csr(oracle, ref_fsai, "cube8_Q"), width=width, step=step)
     vals, bad_diag, bad_rows = oracle.fsai_refit(_csr(oracle, ref_fsai, "cube8_Q2"), g)
     assert bad_diag == 0 and bad_rows == 0
-    np.testing.assert_array_equal(g.columns, ref_fsai["cube8_refit_G_col"])
-    np.testing.assert_array_equal(_bits(vals), _bits(ref_fsai["cube8_refit_G_val"]))
+    np.testing.assert_array_equal(g.columns, ref_fsai[tag + "_G_col"])
+    np.testing.assert_array_equal(_bits(vals), _bits(ref_fsai[tag + "_G_val"]))
 
 
 def test_block_jacobi_and_ilu0(oracle, ref_block):
