@@ -12,7 +12,8 @@ preconditioners on seeded inputs and stores inputs and outputs in
   warp_preconditioners/fsai.py: build kernel, pack_factor, bsr_transposed)
   of the 64 x 64 five-point Laplacian (width 8, step 1), of the assembled
   biharmonic ``Q = alpha M + K M^-1 K`` on an 8^3 jittered tet cube (widths
-  8/16/48/64, steps 1/2, a float32 factor at kap 3e-3), and the
+  8/16/48/64, steps 1/2, a float32 factor at kap 3e-3, and the factor of the
+  same Q rounded to a float32 matrix, built in float32), and the
   fixed-support refit of the width-8 and the width-48 factor for Q at
   2 alpha (``FSAI.update``, warp_preconditioners/fsai_reuse.py).
 * ``ref_block.npz``: on A = K (x) C (K the 7-point Laplacian on 6^3 nodes,
@@ -93,8 +94,9 @@ def fsai_cases():
     verts, tets, K, mass = problems.tet_cube(8)
     Q = problems.biharmonic(K, mass, ALPHA)
     put_csr(out, "cube8_Q", Q.indptr, Q.indices, Q.data)
-    for width, step, kap, fdt in [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 2, 1e-3, None),
-                                  (64, 1, 1e-3, None), (8, 1, 3e-3, wp.float32)]:
+    for width, step, kap, fdt in [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 1, 1e-3, None),
+                                  (48, 2, 1e-3, None), (64, 1, 1e-3, None),
+                                  (8, 1, 3e-3, wp.float32)]:
         t = time.time()
         pre = FSAI(from_scipy(Q), max_row_size=width, kap_tolerance=kap, max_step_size=step,
                    factor_dtype=fdt)
@@ -103,6 +105,17 @@ def fsai_cases():
         put_bsr(out, tag + "_GT", pre.GT)
         out[tag + "_truncated"] = np.int32(pre.truncated_rows)
         print(f"{tag}: nnz {pre.G.nnz} ({time.time() - t:.1f} s)", flush=True)
+
+    # A float32 matrix: the whole build in float32 arithmetic.
+    qf = Q.astype(np.float32)
+    put_csr(out, "cube8_Qf32", qf.indptr, qf.indices, qf.data)
+    t = time.time()
+    pre = FSAI(from_scipy(qf, wp.float32), max_row_size=16, kap_tolerance=1e-3,
+               max_step_size=2)
+    put_bsr(out, "cube8_f32mat_w16s2_G", pre.G)
+    put_bsr(out, "cube8_f32mat_w16s2_GT", pre.GT)
+    out["cube8_f32mat_w16s2_truncated"] = np.int32(pre.truncated_rows)
+    print(f"cube8 float32 matrix w16 s2: nnz {pre.G.nnz} ({time.time() - t:.1f} s)", flush=True)
 
     # Fixed-support refit for new values on the same pattern.
     Q2 = problems.biharmonic(K, mass, 2 * ALPHA)

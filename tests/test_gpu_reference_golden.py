@@ -21,7 +21,7 @@ from gpu_helpers import cuda, host_csr, vec
 
 pytestmark = pytest.mark.gpu
 
-REF_FSAI = [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 2, 1e-3, None),
+REF_FSAI = [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 1, 1e-3, None), (48, 2, 1e-3, None),
             (64, 1, 1e-3, None), (8, 1, 3e-3, torch.float32)]
 
 
@@ -86,6 +86,18 @@ def test_fsai_tet_cube_biharmonic(ref_fsai, width, step, kap, fdt):
     assert_factor_equal(pre.G, ref_fsai, tag + "_G")
     assert_factor_equal(pre.GT, ref_fsai, tag + "_GT")
     assert pre.truncated_rows == int(ref_fsai[tag + "_truncated"])
+
+
+def test_fsai_float32_matrix(ref_fsai):
+    # The build in float32 arithmetic (the float instantiation of the build).
+    from warp_preconditioners_gb300 import FSAI
+
+    q = _matrix(ref_fsai, "cube8_Qf32")
+    assert q.values.dtype == torch.float32
+    pre = FSAI(q, max_row_size=16, kap_tolerance=1e-3, max_step_size=2)
+    assert_factor_equal(pre.G, ref_fsai, "cube8_f32mat_w16s2_G")
+    assert_factor_equal(pre.GT, ref_fsai, "cube8_f32mat_w16s2_GT")
+    assert pre.truncated_rows == int(ref_fsai["cube8_f32mat_w16s2_truncated"])
 
 
 @pytest.mark.parametrize("width,step,tag", [(8, 1, "cube8_refit"), (48, 2, "cube8_refit48")])

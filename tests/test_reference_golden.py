@@ -19,7 +19,7 @@ import pytest
 
 from conftest import GOLDEN
 
-REF_FSAI = [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 2, 1e-3, None),
+REF_FSAI = [(8, 1, 1e-3, None), (16, 2, 1e-3, None), (48, 1, 1e-3, None), (48, 2, 1e-3, None),
             (64, 1, 1e-3, None), (8, 1, 3e-3, np.float32)]
 
 
@@ -87,6 +87,15 @@ def test_fsai_tet_cube_biharmonic(oracle, ref_fsai, width, step, kap, fdt):
     assert_csr_equal(g, ref_fsai, tag + "_G")
     assert_csr_equal(gt, ref_fsai, tag + "_GT")
     assert trunc == int(ref_fsai[tag + "_truncated"])
+
+
+def test_fsai_float32_matrix(oracle, ref_fsai):
+    q = _csr(oracle, ref_fsai, "cube8_Qf32")
+    assert q.values.dtype == np.float32
+    g, gt, trunc = oracle.fsai(q, width=16, step=2, tol=1e-3)
+    assert_csr_equal(g, ref_fsai, "cube8_f32mat_w16s2_G")
+    assert_csr_equal(gt, ref_fsai, "cube8_f32mat_w16s2_GT")
+    assert trunc == int(ref_fsai["cube8_f32mat_w16s2_truncated"])
 
 
 @pytest.mark.parametrize("width,step,tag", [(8, 1, "cube8_refit"), (48, 2, "cube8_refit48")])
