@@ -19,7 +19,8 @@ preconditioners on seeded inputs and stores inputs and outputs in
 * ``ref_block.npz``: on A = K (x) C (K the 7-point Laplacian on 6^3 nodes,
   C = R diag(1, 1, 1e-6) R^T): BlockJacobi inverses
   (warp_preconditioners/block_ilu.py), BlockILU0 factors with 3 factor sweeps
-  and one 3-sweep apply, the scalarised FSAI (width 8, kap 3e-3, float32
+  and one 3-sweep apply, with the defaults (12 / 4 sweeps) and relaxed (6 / 2
+  sweeps, relaxation 0.8), the scalarised FSAI (width 8, kap 3e-3, float32
   factor), and the block FSAI candidate's scalar factor for 2 and 4 blocks
   (benchmarks/block_fsai_candidate.py).
 * ``ref_quality.npz``: ``FSAI.quality`` values (4 probes seed 17, 2 probes
@@ -162,6 +163,16 @@ def block_cases():
     z = wp.zeros_like(xv)
     jac.matvec(xv, yv, z, 0.7, -0.2)
     out["kron6_jacobi_apply"] = z.numpy().reshape(-1).copy()
+    # The reference's defaults (12 factor sweeps, 4 solve sweeps), and a
+    # relaxed factorisation.
+    for tag, kw in (("ilu_default", {}), ("ilu_relaxed", dict(factor_sweeps=6, solve_sweeps=2,
+                                                                   relaxation=0.8))):
+        m = BlockILU0(A, **kw)
+        out[f"kron6_{tag}_factors"] = m.factors.numpy().copy()
+        out[f"kron6_{tag}_inverse"] = m.inverse_diagonal.numpy().copy()
+        z = wp.zeros_like(xv)
+        m.matvec(xv, yv, z, 0.7, -0.2)
+        out[f"kron6_{tag}_apply"] = z.numpy().reshape(-1).copy()
     pre = FSAI(A, max_row_size=8, kap_tolerance=3e-3, factor_dtype=wp.float32)
     put_bsr(out, "kron6_fsai_G", pre.G)
     put_bsr(out, "kron6_fsai_GT", pre.GT)

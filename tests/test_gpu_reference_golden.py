@@ -135,6 +135,24 @@ def test_block_jacobi_and_ilu0(ref_block):
         _close(z.cpu().numpy(), ref_block[key], rtol=1e-9)
 
 
+@pytest.mark.parametrize("tag,fs,ss,relax", [("ilu_default", 12, 4, 1.0),
+                                              ("ilu_relaxed", 6, 2, 0.8)])
+def test_block_ilu0_sweeps_and_relaxation(ref_block, tag, fs, ss, relax):
+    from warp_preconditioners_gb300 import BlockILU0
+
+    A = _matrix(ref_block, "kron6_A", block=3)
+    ilu = BlockILU0(A, factor_sweeps=fs, solve_sweeps=ss, relaxation=relax)
+    np.testing.assert_array_equal(_bits(ilu.factors.cpu().numpy()),
+                                  _bits(ref_block[f"kron6_{tag}_factors"]))
+    np.testing.assert_array_equal(_bits(ilu.inverse_diagonal.cpu().numpy()),
+                                  _bits(ref_block[f"kron6_{tag}_inverse"]))
+    # The apply to 1e-9 of the largest entry, as above.
+    x, y = vec(ref_block["kron6_x"]), vec(ref_block["kron6_y"])
+    z = torch.empty_like(x)
+    ilu.matvec(x, y, z, 0.7, -0.2)
+    _close(z.cpu().numpy(), ref_block[f"kron6_{tag}_apply"], rtol=1e-9)
+
+
 def test_scalarised_and_block_fsai(ref_block):
     from warp_preconditioners_gb300 import FSAI, BlockFSAI
 

@@ -124,6 +124,21 @@ def test_block_jacobi_and_ilu0(oracle, ref_block):
     np.testing.assert_array_equal(_bits(z), _bits(ref_block["kron6_jacobi_apply"]))
 
 
+@pytest.mark.parametrize("tag,fs,ss,relax", [("ilu_default", 12, 4, 1.0),
+                                              ("ilu_relaxed", 6, 2, 0.8)])
+def test_block_ilu0_sweeps_and_relaxation(oracle, ref_block, tag, fs, ss, relax):
+    off, col, val = ref_block["kron6_A_off"], ref_block["kron6_A_col"], ref_block["kron6_A_val"]
+    nrow = len(off) - 1
+    fac, inv, bad = oracle.bilu0_setup(nrow, 3, off, col, val, factor_sweeps=fs,
+                                       relaxation=relax)
+    assert bad == 0
+    np.testing.assert_array_equal(_bits(fac), _bits(ref_block[f"kron6_{tag}_factors"]))
+    np.testing.assert_array_equal(_bits(inv), _bits(ref_block[f"kron6_{tag}_inverse"]))
+    x, y = ref_block["kron6_x"], ref_block["kron6_y"]
+    z = oracle.bilu0_apply(nrow, 3, off, col, fac, inv, ss, x, y, 0.7, -0.2)
+    np.testing.assert_array_equal(_bits(z), _bits(ref_block[f"kron6_{tag}_apply"]))
+
+
 def test_scalarised_and_block_fsai(oracle, ref_block):
     off, col, val = ref_block["kron6_A_off"], ref_block["kron6_A_col"], ref_block["kron6_A_val"]
     nrow = len(off) - 1
