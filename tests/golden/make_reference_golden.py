@@ -12,8 +12,9 @@ preconditioners on seeded inputs and stores inputs and outputs in
   warp_preconditioners/fsai.py: build kernel, pack_factor, bsr_transposed)
   of the 64 x 64 five-point Laplacian (width 8, step 1), of the assembled
   biharmonic ``Q = alpha M + K M^-1 K`` on an 8^3 jittered tet cube (widths
-  8/16/48/64, steps 1/2, a float32 factor at kap 3e-3, and the factor of the
-  same Q rounded to a float32 matrix, built in float32), and the
+  8/16/48/64, steps 1/2, width 48 without a stopping tolerance, a float32
+  factor at kap 3e-3, and the factor of the same Q rounded to a float32
+  matrix, built in float32), and the
   fixed-support refit of the width-8 and the width-48 factor for Q at
   2 alpha (``FSAI.update``, warp_preconditioners/fsai_reuse.py).
 * ``ref_block.npz``: on A = K (x) C (K the 7-point Laplacian on 6^3 nodes,
@@ -22,6 +23,7 @@ preconditioners on seeded inputs and stores inputs and outputs in
   and one 3-sweep apply, with the defaults (12 / 4 sweeps) and relaxed (6 / 2
   sweeps, relaxation 0.8), the scalarised FSAI (width 8, kap 3e-3, float32
   factor), and the block FSAI candidate's scalar factor for 2 and 4 blocks
+  (float64) and 3 blocks (its default float32 storage)
   (benchmarks/block_fsai_candidate.py).
 * ``ref_quality.npz``: ``FSAI.quality`` values (4 probes seed 17, 2 probes
   seed 5) on the 6^3 tet-cube Q and the 32 x 32 Laplacian with their
@@ -107,6 +109,15 @@ def fsai_cases():
         out[tag + "_truncated"] = np.int32(pre.truncated_rows)
         print(f"{tag}: nnz {pre.G.nnz} ({time.time() - t:.1f} s)", flush=True)
 
+    # No stopping tolerance: every row grows until its frontier or the
+    # width runs out.
+    t = time.time()
+    pre = FSAI(from_scipy(Q), max_row_size=48, kap_tolerance=0.0, max_step_size=1)
+    put_bsr(out, "cube8_w48s1_kap0_G", pre.G)
+    put_bsr(out, "cube8_w48s1_kap0_GT", pre.GT)
+    out["cube8_w48s1_kap0_truncated"] = np.int32(pre.truncated_rows)
+    print(f"cube8 w48 s1 kap 0: nnz {pre.G.nnz} ({time.time() - t:.1f} s)", flush=True)
+
     # A float32 matrix: the whole build in float32 arithmetic.
     qf = Q.astype(np.float32)
     put_csr(out, "cube8_Qf32", qf.indptr, qf.indices, qf.data)
@@ -180,6 +191,10 @@ def block_cases():
         bf = BlockFSAI(A, max_blocks=blocks, factor_dtype=wp.float64)
         put_bsr(out, f"kron6_bfsai{blocks}_G", bf.G)
         put_bsr(out, f"kron6_bfsai{blocks}_GT", bf.GT)
+    # Three blocks with the candidate's default float32 factor storage.
+    bf = BlockFSAI(A, max_blocks=3)
+    put_bsr(out, "kron6_bfsai3_f32_G", bf.G)
+    put_bsr(out, "kron6_bfsai3_f32_GT", bf.GT)
     np.savez_compressed(HERE / "ref_block.npz", **out)
     print("block cases done", flush=True)
 

@@ -100,6 +100,17 @@ def test_fsai_float32_matrix(ref_fsai):
     assert pre.truncated_rows == int(ref_fsai["cube8_f32mat_w16s2_truncated"])
 
 
+def test_fsai_without_stopping_tolerance(ref_fsai):
+    # Every row grows until its frontier or the width runs out.
+    from warp_preconditioners_gb300 import FSAI
+
+    pre = FSAI(_matrix(ref_fsai, "cube8_Q"), max_row_size=48, kap_tolerance=0.0,
+               max_step_size=1)
+    assert_factor_equal(pre.G, ref_fsai, "cube8_w48s1_kap0_G")
+    assert_factor_equal(pre.GT, ref_fsai, "cube8_w48s1_kap0_GT")
+    assert pre.truncated_rows == int(ref_fsai["cube8_w48s1_kap0_truncated"])
+
+
 @pytest.mark.parametrize("width,step,tag", [(8, 1, "cube8_refit"), (48, 2, "cube8_refit48")])
 def test_fsai_refit(ref_fsai, width, step, tag):
     # Width 48 runs the wide refit (a thread per row, factors in device memory).
@@ -164,6 +175,9 @@ def test_scalarised_and_block_fsai(ref_block):
         bf = BlockFSAI(A, max_blocks=blocks, factor_dtype=torch.float64)
         assert_factor_equal(bf.G, ref_block, f"kron6_bfsai{blocks}_G")
         assert_factor_equal(bf.GT, ref_block, f"kron6_bfsai{blocks}_GT")
+    bf = BlockFSAI(A, max_blocks=3)  # the default float32 storage
+    assert_factor_equal(bf.G, ref_block, "kron6_bfsai3_f32_G")
+    assert_factor_equal(bf.GT, ref_block, "kron6_bfsai3_f32_GT")
 
 
 def test_factored_operator_and_fsai_apply(ref_ops, ref_fsai):

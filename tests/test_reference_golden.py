@@ -98,6 +98,14 @@ def test_fsai_float32_matrix(oracle, ref_fsai):
     assert trunc == int(ref_fsai["cube8_f32mat_w16s2_truncated"])
 
 
+def test_fsai_without_stopping_tolerance(oracle, ref_fsai):
+    q = _csr(oracle, ref_fsai, "cube8_Q")
+    g, gt, trunc = oracle.fsai(q, width=48, step=1, tol=0.0)
+    assert_csr_equal(g, ref_fsai, "cube8_w48s1_kap0_G")
+    assert_csr_equal(gt, ref_fsai, "cube8_w48s1_kap0_GT")
+    assert trunc == int(ref_fsai["cube8_w48s1_kap0_truncated"])
+
+
 @pytest.mark.parametrize("width,step,tag", [(8, 1, "cube8_refit"), (48, 2, "cube8_refit48")])
 def test_fsai_refit(oracle, ref_fsai, width, step, tag):
     g, _, _ = oracle.fsai(_csr(oracle, ref_fsai, "cube8_Q"), width=width, step=step)
@@ -152,6 +160,13 @@ def test_scalarised_and_block_fsai(oracle, ref_block):
         g = oracle.fsai_pack(3 * nrow, 3 * blocks, cols, vals)
         assert_csr_equal(g, ref_block, f"kron6_bfsai{blocks}_G")
         assert_csr_equal(oracle.transpose(g), ref_block, f"kron6_bfsai{blocks}_GT")
+    # Three blocks, the candidate's default float32 storage.
+    cols, vals, _, bad = oracle.block_fsai_setup(nrow, 3, 3, off, col, val)
+    assert bad == 0
+    g = oracle.fsai_pack(3 * nrow, 9, cols, vals)
+    g = oracle.CSR(g.offsets, g.columns, g.values.astype(np.float32))
+    assert_csr_equal(g, ref_block, "kron6_bfsai3_f32_G")
+    assert_csr_equal(oracle.transpose(g), ref_block, "kron6_bfsai3_f32_GT")
 
 
 def test_factored_operator_and_fsai_apply(oracle, ref_ops, ref_fsai):
